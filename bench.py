@@ -1,0 +1,357 @@
+#!/usr/bin/env python
+"""Benchmark of the SPH substep pipeline on GB300.
+
+Default workload: the 1,048,576-particle dam break (128x64x128 lattice at
+spacing 0.1 in a 25.6x12.8x25.6 box, r 0.175, dt 1/120 in 2 substeps). One
+step = one dt = 2 substeps = one FluidSimBase::update(dt).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints ONE JSON line (rank 0). `value` = particle-steps/s of the whole job
+with the state resident in HBM (CUDA events on the library's stream, L2
+flushed before every timed step); `e2e` = the same metric through the public
+API with the state in pinned host memory (upload + step + download every
+step). For N>1 every rank runs an independent replica of the scene (the path
+has no cross-scene exchange): weak scaling, max time over ranks.
+
+--impl reference times the reference CPU implementation of the path on the
+host cores (the oracle's restatement, all hardware threads; the reference's
+own build where it exists here) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+PKG = ROOT / "fluid-simulation-3d_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s"
+UNIT = "particle-steps/s"
+# Compulsory unique bytes per particle of each kernel of a substep (reads +
+# writes of its inputs and outputs once), for the roofline.
+ALG_BYTES = {
+    "predict_hash": 44,   # pos 16 + vel 16 in; key/rank 8 + count 4 out
+    "spatial": 132,       # scan 12 + scatter 24 + reorder 96
+    "density": 44,        # pred 16 + start 4 in; dens_a 8 + dens_b 16 out
+    "pressure": 76,       # pred 16, start 4, dens_a 8, dens_b 16, vel 16 in; velp 16 out
+    "viscosity": 84,      # pred 16, start 4, velp 16, pos 16 in; pos 16 + vel 16 out
+}
+SURVEY_BYTES_PER_SUBSTEP = 300  # idealised whole-substep traffic per particle
+PHASES = ["predict_hash", "spatial", "density", "pressure", "viscosity"]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["native", "reference"], default="native")
+    ap.add_argument("--workload", default="dam_break_1m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(ROOT / "MEASURED_PEAKS.json") as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(workload, kernel):
+    """DRAM bytes per launch per particle from a committed ncu summary."""
+    try:
+        with open(ROOT / "profiles" / "dram_traffic.json") as f:
+            d = json.load(f)
+        return d[workload][kernel]
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed
+    region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.tmp.flush()
+        self.tmp.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.tmp.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.tmp.name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_workload(name):
+    from fluidsim import scenes
+    if name not in scenes.WORKLOADS:
+        raise SystemExit(f"unknown workload {name}")
+    return scenes.WORKLOADS[name]()
+
+
+def cpu_port_rate(sc, max_steps, budget_s, threads=0):
+    """Oracle restatement (Jacobi, all host threads) on the full scene: returns
+    (particle-steps/s, steps timed, seconds, threads)."""
+    import oracle
+    oracle.build()
+    p, n, S = sc["params"], sc["pos"].shape[0], sc["substeps"]
+    dt = np.float32(np.float32(sc["dt"]) / np.float32(S))
+    pos, vel = sc["pos"].copy(), sc["vel"].copy()
+    th = threads or oracle.hw_threads()
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        for _ in range(S):
+            pos, vel, _ = oracle.substep_f32(p, pos, vel, dt, nthreads=th, debug=False)
+        steps += 1
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    el = time.perf_counter() - t0
+    return n * steps / el, steps, el, th
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sc = load_workload(args.workload)
+    n = sc["pos"].shape[0]
+    # warm-up is one substep of the same scene
+    import oracle
+    oracle.build()
+    th = oracle.hw_threads()
+    dt = np.float32(np.float32(sc["dt"]) / np.float32(sc["substeps"]))
+    for _ in range(min(args.warmup, 1)):
+        oracle.substep_f32(sc["params"], sc["pos"], sc["vel"], dt, nthreads=th, debug=False)
+    rate, steps, el, th = cpu_port_rate(sc, args.steps, budget_s=150.0, threads=th)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "steps_timed": steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded dam-break lattice)",
+        "config": {"workload": args.workload, "particles": n,
+                   "substeps": sc["substeps"], "dt": sc["dt"]},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": th, "kind": "port",
+                         "sample": f"{steps} full steps ({steps * sc['substeps']} "
+                                   f"substeps) of the {n}-particle scene, Jacobi "
+                                   f"restatement of physicsWorld.cc:39-111 on {th} threads"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_native(args):
+    import torch
+    import torch.distributed as tdist
+
+    import build_lib
+    import fluidsim
+
+    rank, world, local = dist_env()
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device (no CPU fallback)")
+    torch.cuda.set_device(local)
+    if world > 1:
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if not fluidsim.LIB_PATH.exists():
+        build_lib.build()
+    sc = load_workload(args.workload)
+    n = sc["pos"].shape[0]
+    S = sc["substeps"]
+    dt = float(sc["dt"])
+    stream = torch.cuda.current_stream()
+    sim = fluidsim.FluidSimulation(sc["params"], stream=stream)
+    sim.InitializeData(n, sc["pos"], sc["vel"])
+    sim.profile_enable(True)
+
+    for _ in range(args.warmup):
+        sim.step_async(dt, S)
+    torch.cuda.synchronize()
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    phase = np.zeros(6)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = sim.kernel_launches()
+    if world > 1:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()  # L2 flush between timed steps (outside the events)
+        ev0[k].record(stream)
+        sim.step_async(dt, S)
+        ev1[k].record(stream)
+        phase += np.array(sim.phase_times())
+    torch.cuda.synchronize()
+    if world > 1:
+        tdist.barrier()
+    wall = time.perf_counter() - wall0
+    launches = sim.kernel_launches() - launches0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    total_ms = float(sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * args.steps / (total_ms / 1000.0)
+    assert sim.status() == 0, "device status flags raised"
+
+    # --- e2e through the public API with the state in pinned host memory
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    pos_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    vel_h = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    pos_h[:] = sc["pos"]
+    vel_h[:] = sc["vel"]
+    dens_h = None
+    torch.cuda.synchronize()
+    if world > 1:
+        tdist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.upload(pos_h, vel_h)
+        sim.step_async(dt, S)
+        check = sim._lib.sph_download(sim.handle, pos_h.ctypes.data,
+                                      vel_h.ctypes.data, dens_h, sim._stream)
+        if check != 0:
+            raise RuntimeError("download failed")
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * n * e2e_steps / e2e_s
+    sim.close()
+
+    if rank != 0:
+        if world > 1:
+            tdist.destroy_process_group()
+        return 0
+
+    # roofline of the dominant kernel (per launch, from live CUDA events)
+    names = ["predict_hash", "spatial", "density", "pressure", "viscosity"]
+    launches_per_phase = {"predict_hash": args.steps, "spatial": args.steps * S,
+                          "density": args.steps * S, "pressure": args.steps * S,
+                          "viscosity": args.steps * S}
+    per_launch_ms = {nm: phase[i] / launches_per_phase[nm] for i, nm in enumerate(names)}
+    share = {nm: phase[i] / max(phase[:5].sum(), 1e-12) for i, nm in enumerate(names)}
+    dom = max(["density", "pressure", "viscosity"], key=lambda k: per_launch_ms[k])
+    peak, peak_kind = peaks()
+    achieved = ALG_BYTES[dom] * n / (per_launch_ms[dom] / 1000.0) / 1e9
+    tr = ncu_traffic(args.workload, dom)
+    ms_step = total_ms / args.steps
+    sub_ms = ms_step / S
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded dam-break lattice, no dataset)",
+        "config": {"workload": args.workload, "particles": n, "substeps": S,
+                   "dt": dt, "parallelism": f"replicas{world}" if world > 1 else "single",
+                   "l2": "flushed (256 MiB write) before every timed step"},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind,
+                     "alg_bytes_per_particle": ALG_BYTES[dom],
+                     "traffic": (tr * n if tr is not None else None)},
+        "substep": {"ms": sub_ms,
+                    "alg_GBps_at_300B": SURVEY_BYTES_PER_SUBSTEP * n / (sub_ms / 1000) / 1e9,
+                    "frac_at_300B": SURVEY_BYTES_PER_SUBSTEP * n / (sub_ms / 1000) / 1e9 / peak,
+                    "phase_ms_per_launch": per_launch_ms, "phase_share": share},
+        "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
+                "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n},
+        "wall_s": wall,
+    }
+    if clk:
+        line["clocks"] = clk
+    if not args.no_cpu_baseline and world == 1:
+        rate, steps, el, th = cpu_port_rate(sc, max_steps=4, budget_s=8.0)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": th, "kind": "port",
+            "sample": f"{steps} full steps of the {n}-particle scene "
+                      f"({steps * S} substeps), {el:.1f} s on {th} threads"}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        tdist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_native(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

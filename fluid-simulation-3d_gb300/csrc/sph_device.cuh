@@ -1,0 +1,94 @@
+// Device-side definitions shared by the SPH kernels (sm_103a).
+//
+// Layout in HBM (one engine, S scenes concatenated, capacity P particles):
+//   pos[P], vel[P]      float4 state in the current sorted layout; pos.w holds
+//                       the particle's global id as raw bits
+//   pred[P]             float4 (predicted position, float(cell hash))
+//   dens_a[P]           float2 (density, near density)
+//   dens_b[P]           float4 (1/rho, P/rho, 1/rho_n, Pn/rho_n)
+//   velp[P]             float4 post-pressure velocity (Jacobi snapshot)
+//   keyrank[P]          uint2 (global key, arrival rank in the key bucket)
+//   tmp[P]              uint2 (id, source slot) bucketed, pre-canonical
+//   count[P], start[P+1] uint32 counting-sort table; a scene owns keys
+//                       [base, base+n) so start[] is also its slot range
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sph {
+
+// Hash multipliers of HashCell (engine/physics/physicsWorld.cc:507-509).
+constexpr uint32_t kHashX = 15823u;
+constexpr uint32_t kHashY = 9737333u;
+constexpr uint32_t kHashZ = 440817757u;
+
+// Particles per tile: one warp. Tiles never straddle scenes.
+constexpr int kTile = 32;
+
+// Per-scene descriptor, built on the host from sph_params.
+struct SceneDev {
+  uint32_t n;         // particles (and key-table size: key = hash % n)
+  uint32_t base;      // first slot of the scene's current layout / table
+  uint64_t fm;        // Lemire magic for x % n
+  float r;            // interaction radius
+  float cut_lt;       // d2 <= cut_lt  <=>  d2 <= sqrRadius && sqrtf(d2) < r
+  float cut_le;       // d2 <= cut_le  <=>  d2 <= sqrRadius && sqrtf(d2) <= r
+  float r2;           // r*r
+  float vol2, vol3;   // density kernel scales   (kernels.h:28,40)
+  float ds2h, ds3h;   // 0.5 * derivative scales (kernels.h:52,64)
+  float vscale;       // poly6 scale             (kernels.h:76)
+  float rho0, k, kn, mu;
+  float gy;           // -gravityScale if gravity else 0   (:313-323)
+  float hx, hy, hz;   // BoundScale * 0.5                   (:88)
+  float ndamp;        // -1 * dampFactor                    (:94)
+  float pdt;          // prediction look-ahead 1/120        (:47)
+  float dt;           // substep dt
+};
+
+// x % d for 32-bit x, d >= 1, with M = floor((2^64-1)/d) + 1 (Lemire et al.,
+// "Faster Remainder by Direct Computation", 2019).
+__device__ __forceinline__ uint32_t fastmod(uint32_t x, uint64_t M,
+                                            uint32_t d) {
+  const uint64_t low = M * static_cast<uint64_t>(x);
+  return static_cast<uint32_t>(__umul64hi(low, static_cast<uint64_t>(d)));
+}
+
+// Gravity + prediction of physicsWorld.cc:45-47 with the reference's
+// rounding (separate multiply and add, no FMA contraction).
+__device__ __forceinline__ void predict(const SceneDev& S, float4 p, float4 v,
+                                        float3& vn, float3& pr) {
+  vn.x = __fadd_rn(v.x, __fmul_rn(0.0f, S.dt));
+  vn.y = __fadd_rn(v.y, __fmul_rn(S.gy, S.dt));
+  vn.z = __fadd_rn(v.z, __fmul_rn(0.0f, S.dt));
+  pr.x = __fadd_rn(p.x, __fmul_rn(vn.x, S.pdt));
+  pr.y = __fadd_rn(p.y, __fmul_rn(vn.y, S.pdt));
+  pr.z = __fadd_rn(p.z, __fmul_rn(vn.z, S.pdt));
+}
+
+// PositionToCellCoord (physicsWorld.cc:499-503): floor of the IEEE quotient.
+__device__ __forceinline__ int cell_of(float p, float r) {
+  return static_cast<int>(floorf(__fdiv_rn(p, r)));
+}
+
+// HashCell (physicsWorld.cc:505-511); the float->uint32 cast wraps modulo
+// 2^32 as on x86-64.
+__device__ __forceinline__ uint32_t hash_cell(int cx, int cy, int cz) {
+  return static_cast<uint32_t>(cx) * kHashX + static_cast<uint32_t>(cy) * kHashY +
+         static_cast<uint32_t>(cz) * kHashZ;
+}
+
+__device__ __forceinline__ uint32_t hash_of(const SceneDev& S, float3 pr) {
+  return hash_cell(cell_of(pr.x, S.r), cell_of(pr.y, S.r), cell_of(pr.z, S.r));
+}
+
+// Hash delta of the neighbour offset o in the reference's table order
+// (physicsWorld.h:131-143: dx outermost, dz innermost):
+// hash(c + d) = hash(c) + dx*kHashX + dy*kHashY + dz*kHashZ (mod 2^32).
+__device__ __forceinline__ uint32_t offset_delta(int o) {
+  const int dx = o / 9 - 1, dy = (o / 3) % 3 - 1, dz = o % 3 - 1;
+  return static_cast<uint32_t>(dx) * kHashX + static_cast<uint32_t>(dy) * kHashY +
+         static_cast<uint32_t>(dz) * kHashZ;
+}
+
+}  // namespace sph

@@ -1,0 +1,647 @@
+// Host engine of the SPH substep pipeline (see sph_engine.h).
+#include "sph_engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+namespace sph {
+
+namespace {
+
+constexpr float kPiF = 3.14159265358979323846f;  // glm::pi<float>()
+
+template <class Pred> float LargestWith(float r, Pred ok) {
+  // Largest float x >= 0 with ok(sqrtf(x)), for a monotone predicate on
+  // the correctly rounded square root.
+  float x = r * r;
+  if (!std::isfinite(x)) return std::numeric_limits<float>::max();
+  while (x > 0.0f && !ok(std::sqrt(x))) x = std::nextafter(x, 0.0f);
+  for (;;) {
+    const float y = std::nextafter(x, std::numeric_limits<float>::infinity());
+    if (!ok(std::sqrt(y))) break;
+    x = y;
+  }
+  return x;
+}
+
+SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base,
+                      float sub_dt) {
+  SceneDev d{};
+  d.n = n;
+  d.base = base;
+  d.fm = (~static_cast<uint64_t>(0)) / n + 1;
+  const float r = p.radius;
+  d.r = r;
+  const float t_lt = LargestWith(r, [r](float s) { return s < r; });
+  const float t_le = LargestWith(r, [r](float s) { return s <= r; });
+  d.cut_lt = std::min(p.cutoff_sq, t_lt);
+  d.cut_le = std::min(p.cutoff_sq, t_le);
+  d.r2 = r * r;
+  // kernels.h:28,40,52,64,76 -- same float expressions.
+  d.vol2 = 15.0f / (2.0f * kPiF * powf(r, 5.0f));
+  d.vol3 = 15.0f / (kPiF * powf(r, 6.0f));
+  d.ds2h = 0.5f * (15.0f / (powf(r, 5.0f) * kPiF));
+  d.ds3h = 0.5f * (45.0f / (powf(r, 6.0f) * kPiF));
+  d.vscale = 315.0f / (64.0f * kPiF * powf(std::fabs(r), 9.0f));
+  d.rho0 = p.target_density;
+  d.k = p.pressure_mult;
+  d.kn = p.near_pressure_mult;
+  d.mu = p.viscosity;
+  d.gy = p.gravity_on ? -p.gravity_scale : 0.0f;
+  d.hx = p.bound[0] * 0.5f;
+  d.hy = p.bound[1] * 0.5f;
+  d.hz = p.bound[2] * 0.5f;
+  d.ndamp = -1.0f * p.damping;
+  d.pdt = p.predict_dt;
+  d.dt = sub_dt;
+  return d;
+}
+
+template <class T> cudaError_t Alloc(T** p, uint64_t count) {
+  return cudaMalloc(reinterpret_cast<void**>(p),
+                    std::max<uint64_t>(count, 1) * sizeof(T));
+}
+
+}  // namespace
+
+Engine::Engine(uint64_t capacity, uint32_t max_scenes)
+    : capacity_(capacity), max_scenes_(max_scenes) {
+  scenes_.resize(max_scenes);
+  old_base_.assign(max_scenes, 0);
+}
+
+Engine::~Engine() {
+  ReleaseGraphs();
+  for (auto& e : prof_ev_)
+    if (e) cudaEventDestroy(e);
+  void* ptrs[] = {d_scenes_, d_tiles_old_, d_tiles_new_, d_pos_[0], d_pos_[1],
+                  d_vel_[0], d_vel_[1], ctx_.pred, ctx_.velp, ctx_.dens_a,
+                  ctx_.dens_b, ctx_.keyrank, ctx_.tmp, ctx_.count, ctx_.start,
+                  ctx_.partial, d_out4_, d_status_, d_dbg_hash_, d_dbg_key_,
+                  d_dbg_accp_, d_dbg_velv_, d_dbg_velp_, d_dbg_start_,
+                  d_dbg_scratch_};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+int Engine::Fail(int code, const std::string& msg) {
+  err_ = msg;
+  return code;
+}
+
+int Engine::CudaFail(cudaError_t e, const char* what) {
+  err_ = std::string(what) + ": " + cudaGetErrorString(e);
+  return SPH_ERR_CUDA;
+}
+
+#define SPH_CUDA(call, what)                       \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return CudaFail(e_, what); \
+  } while (0)
+
+int Engine::Init() {
+  if (capacity_ == 0 || capacity_ >= (1ull << 31) || max_scenes_ == 0 ||
+      max_scenes_ >= (1u << kTileSceneBits))
+    return Fail(SPH_ERR_INVALID, "capacity must be in [1, 2^31) and scenes in [1, 2^27)");
+  int dev = 0;
+  SPH_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  SPH_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, dev),
+           "cudaDeviceGetAttribute");
+  const uint64_t C = capacity_;
+  const uint64_t max_tiles = C / kTile + max_scenes_ + 1;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+  chk(Alloc(&d_scenes_, max_scenes_));
+  chk(Alloc(&d_tiles_old_, max_tiles));
+  chk(Alloc(&d_tiles_new_, max_tiles));
+  for (int b = 0; b < 2; ++b) {
+    chk(Alloc(&d_pos_[b], C));
+    chk(Alloc(&d_vel_[b], C));
+  }
+  chk(Alloc(&ctx_.pred, C));
+  chk(Alloc(&ctx_.velp, C));
+  chk(Alloc(&ctx_.dens_a, C));
+  chk(Alloc(&ctx_.dens_b, C));
+  chk(Alloc(&ctx_.keyrank, C));
+  chk(Alloc(&ctx_.tmp, C));
+  chk(Alloc(&ctx_.count, C));
+  chk(Alloc(&ctx_.start, C + 1));
+  chk(Alloc(&ctx_.partial, scan_partials_needed(C)));
+  chk(Alloc(&d_out4_, C));
+  chk(Alloc(&d_status_, 1));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation
+               ? Fail(SPH_ERR_NOMEM, "device allocation failed")
+               : CudaFail(e, "cudaMalloc");
+  }
+  SPH_CUDA(cudaMemset(ctx_.count, 0, C * sizeof(uint32_t)), "cudaMemset");
+  SPH_CUDA(cudaMemset(ctx_.dens_a, 0, C * sizeof(float2)), "cudaMemset");
+  SPH_CUDA(cudaMemset(d_status_, 0, sizeof(uint32_t)), "cudaMemset");
+  SPH_CUDA(cudaMemset(d_out4_, 0, C * sizeof(float4)), "cudaMemset");
+  ctx_.scenes = d_scenes_;
+  ctx_.out4 = d_out4_;
+  ctx_.status = d_status_;
+  return SPH_OK;
+}
+
+uint32_t Engine::NumScenes() const {
+  uint32_t c = 0;
+  for (const auto& s : scenes_) c += s.live ? 1 : 0;
+  return c;
+}
+
+uint64_t Engine::NumParticles() const {
+  uint64_t c = 0;
+  for (const auto& s : scenes_) c += s.live ? s.n : 0;
+  return c;
+}
+
+uint32_t Engine::SceneSize(uint32_t id) const {
+  return (id < max_scenes_ && scenes_[id].live) ? scenes_[id].n : 0;
+}
+
+int Engine::AddScene(const sph_params& p, uint32_t n, const float* pos3,
+                     const float* vel3, bool device_ptrs, float dt,
+                     uint32_t* id, cudaStream_t st) {
+  if (n == 0 || n >= (1u << 24))
+    return Fail(SPH_ERR_INVALID, "scene size must be in [1, 2^24)");
+  if (!(p.radius > 0.0f) || !std::isfinite(p.radius))
+    return Fail(SPH_ERR_INVALID, "radius must be positive and finite");
+  if (layout_total_ + n > capacity_)
+    return Fail(SPH_ERR_NOMEM, "scene does not fit the engine capacity");
+  uint32_t s = 0;
+  while (s < max_scenes_ && scenes_[s].used) ++s;
+  if (s == max_scenes_) return Fail(SPH_ERR_NOMEM, "no free scene slot");
+  Scene& sc = scenes_[s];
+  sc = Scene{};
+  sc.used = sc.live = true;
+  sc.prm = p;
+  sc.n = n;
+  sc.dt = dt;
+  old_base_[s] = static_cast<uint32_t>(layout_total_);
+  layout_total_ += n;
+  layout_dirty_ = scenes_dirty_ = true;
+  const int rc = Load(s, pos3, vel3, device_ptrs, st);
+  if (rc != SPH_OK) {
+    sc = Scene{};
+    layout_total_ -= n;
+    return rc;
+  }
+  if (id) *id = s;
+  return SPH_OK;
+}
+
+int Engine::RemoveScene(uint32_t id) {
+  if (id >= max_scenes_ || !scenes_[id].live)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  scenes_[id].live = false;  // its slots vanish at the next step's sort
+  layout_dirty_ = scenes_dirty_ = true;
+  return SPH_OK;
+}
+
+int Engine::SetParams(uint32_t id, const sph_params& p) {
+  if (id >= max_scenes_ || !scenes_[id].live)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  if (!(p.radius > 0.0f) || !std::isfinite(p.radius))
+    return Fail(SPH_ERR_INVALID, "radius must be positive and finite");
+  scenes_[id].prm = p;
+  scenes_dirty_ = true;
+  return SPH_OK;
+}
+
+int Engine::GetParams(uint32_t id, sph_params* p) const {
+  if (id >= max_scenes_ || !scenes_[id].live || !p) return SPH_ERR_INVALID;
+  *p = scenes_[id].prm;
+  return SPH_OK;
+}
+
+int Engine::SetDt(uint32_t id, float dt) {
+  if (id >= max_scenes_ || !scenes_[id].live)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  if (scenes_[id].dt != dt) {
+    scenes_[id].dt = dt;
+    scenes_dirty_ = true;
+  }
+  return SPH_OK;
+}
+
+int Engine::Load(uint32_t id, const float* pos3, const float* vel3,
+                 bool device_ptrs, cudaStream_t st) {
+  if (id >= max_scenes_ || !scenes_[id].live)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  // pos3 == nullptr loads the zero state (InitializeData, physicsWorld.cc:129-137).
+  const uint32_t n = scenes_[id].n;
+  const float* dp = pos3;
+  const float* dv = vel3;
+  if (!device_ptrs && pos3) {
+    // Stage through the prediction / post-pressure buffers (rewritten by
+    // every substep before use).
+    float* sp = reinterpret_cast<float*>(ctx_.pred);
+    float* sv = reinterpret_cast<float*>(ctx_.velp);
+    SPH_CUDA(cudaMemcpyAsync(sp, pos3, sizeof(float) * 3 * n,
+                             cudaMemcpyHostToDevice, st), "upload positions");
+    if (vel3)
+      SPH_CUDA(cudaMemcpyAsync(sv, vel3, sizeof(float) * 3 * n,
+                               cudaMemcpyHostToDevice, st), "upload velocities");
+    dp = sp;
+    dv = vel3 ? sv : nullptr;
+  } else if (!pos3) {
+    dv = nullptr;
+  }
+  SPH_CUDA(launch_import(old_base_[id], n, dp, dv, d_pos_[cur_], d_vel_[cur_], st),
+           "import kernel");
+  // Densities are unknown until the next step.
+  SPH_CUDA(cudaMemsetAsync(ctx_.dens_a + old_base_[id], 0, sizeof(float2) * n, st),
+           "cudaMemsetAsync");
+  debug_valid_ = false;
+  return SPH_OK;
+}
+
+void Engine::BuildTiles(std::vector<uint2>& out, bool old_layout) const {
+  out.clear();
+  for (uint32_t s = 0; s < max_scenes_; ++s) {
+    const Scene& sc = scenes_[s];
+    if (!sc.live) continue;
+    const uint32_t b = old_layout ? old_base_[s] : sc.base;
+    for (uint32_t f = 0; f < sc.n; f += kTile)
+      out.push_back(make_tile(s, b + f, std::min<uint32_t>(kTile, sc.n - f)));
+  }
+}
+
+int Engine::BuildLayout(cudaStream_t st) {
+  if (!layout_dirty_) return SPH_OK;
+  uint32_t b = 0;
+  for (uint32_t s = 0; s < max_scenes_; ++s) {
+    Scene& sc = scenes_[s];
+    if (!sc.live) continue;
+    sc.base = b;
+    b += sc.n;
+  }
+  total_ = b;
+  std::vector<uint2> t_old, t_new;
+  BuildTiles(t_old, true);
+  BuildTiles(t_new, false);
+  n_tiles_old_ = static_cast<uint32_t>(t_old.size());
+  n_tiles_new_ = static_cast<uint32_t>(t_new.size());
+  if (n_tiles_old_)
+    SPH_CUDA(cudaMemcpyAsync(d_tiles_old_, t_old.data(), sizeof(uint2) * n_tiles_old_,
+                             cudaMemcpyHostToDevice, st), "upload tiles");
+  if (n_tiles_new_)
+    SPH_CUDA(cudaMemcpyAsync(d_tiles_new_, t_new.data(), sizeof(uint2) * n_tiles_new_,
+                             cudaMemcpyHostToDevice, st), "upload tiles");
+  // The host vectors die at return: make the copies complete first.
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  ReleaseGraphs();
+  scenes_dirty_ = true;
+  return SPH_OK;
+}
+
+int Engine::UploadScenes(int substeps, cudaStream_t st) {
+  if (!scenes_dirty_ && uploaded_substeps_ == substeps) return SPH_OK;
+  std::vector<SceneDev> h(max_scenes_);
+  uint32_t hi = 0;
+  for (uint32_t s = 0; s < max_scenes_; ++s) {
+    const Scene& sc = scenes_[s];
+    if (!sc.live) continue;
+    h[s] = MakeSceneDev(sc.prm, sc.n, sc.base, sc.dt / static_cast<float>(substeps));
+    hi = s + 1;
+  }
+  if (hi)
+    SPH_CUDA(cudaMemcpyAsync(d_scenes_, h.data(), sizeof(SceneDev) * hi,
+                             cudaMemcpyHostToDevice, st), "upload scenes");
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  scenes_dirty_ = false;
+  uploaded_substeps_ = substeps;
+  return SPH_OK;
+}
+
+// Launches `substeps` substeps starting from state buffers cur_. Does not
+// change engine state, so it can run under stream capture.
+int Engine::RunSubsteps(int substeps, cudaStream_t st) {
+  LaunchCtx c = ctx_;
+  c.block_nbr = tuning_.block;
+  c.max_blocks = 0;
+  c.src_limit = static_cast<uint32_t>(capacity_);
+  int cur = cur_;
+  const Tiles told{d_tiles_old_, n_tiles_old_};
+  const Tiles tnew{d_tiles_new_, n_tiles_new_};
+  for (int ss = 0; ss < substeps; ++ss) {
+    c.pos = d_pos_[cur];
+    c.vel = d_vel_[cur];
+    c.pos2 = d_pos_[1 - cur];
+    c.vel2 = d_vel_[1 - cur];
+    const bool dbg = debug_ && ss == 0;
+    c.dbg_hash = dbg ? d_dbg_hash_ : nullptr;
+    c.dbg_key = dbg ? d_dbg_key_ : nullptr;
+    c.dbg_accp = dbg ? d_dbg_accp_ : nullptr;
+    c.dbg_velv = dbg ? d_dbg_velv_ : nullptr;
+    const Tiles& first = ss == 0 ? told : tnew;
+    cudaEvent_t* ev = profile_ ? &prof_ev_[ss * kPhaseEvents] : nullptr;
+    cudaError_t e = cudaSuccess;
+    auto mark = [&](int k) {
+      if (ev && e == cudaSuccess) e = cudaEventRecord(ev[k], st);
+    };
+    mark(0);
+    if (ss == 0) e = launch_predict_hash(c, first, st);
+    mark(1);
+    if (e == cudaSuccess) e = launch_scan(c, total_, st);
+    if (e == cudaSuccess) e = launch_sort_reorder(c, first, tnew, total_, st);
+    mark(2);
+    if (e == cudaSuccess && dbg) {
+      e = cudaMemcpyAsync(d_dbg_start_, c.start, sizeof(uint32_t) * (total_ + 1),
+                          cudaMemcpyDeviceToDevice, st);
+    }
+    if (e == cudaSuccess) e = launch_density(c, tnew, st);
+    mark(3);
+    if (e == cudaSuccess) e = launch_pressure(c, tnew, st);
+    mark(4);
+    if (e == cudaSuccess)
+      e = launch_visc_integrate(c, tnew, ss + 1 < substeps ? 1 : 0,
+                                ss + 1 == substeps ? 1 : 0, st);
+    mark(5);
+    if (e == cudaSuccess && dbg)
+      e = cudaMemcpyAsync(d_dbg_velp_, c.velp, sizeof(float4) * total_,
+                          cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return CudaFail(e, "substep launch");
+    cur = 1 - cur;
+  }
+  return SPH_OK;
+}
+
+int Engine::ProfileEnable(bool on) {
+  if (on && prof_ev_.empty()) {
+    prof_ev_.resize(kPhaseEvents * kMaxSubsteps);
+    for (auto& e : prof_ev_) SPH_CUDA(cudaEventCreate(&e), "cudaEventCreate");
+  }
+  if (on != profile_) ReleaseGraphs();
+  profile_ = on;
+  profiled_substeps_ = 0;
+  return SPH_OK;
+}
+
+// ms per phase of the last step, summed over its substeps, in the order of
+// the reference's timers (Gravity, Spatial, Density, Pressure, Viscosity,
+// PosNColl; physicsWorld.h:45-50). Integration and collision run inside the
+// viscosity kernel, so PosNColl is reported as 0.
+int Engine::PhaseTimes(double out[6]) {
+  for (int k = 0; k < 6; ++k) out[k] = 0.0;
+  if (!profile_ || profiled_substeps_ == 0)
+    return Fail(SPH_ERR_STATE, "profiling not enabled or no step run");
+  for (int ss = 0; ss < profiled_substeps_; ++ss) {
+    cudaEvent_t* ev = &prof_ev_[ss * kPhaseEvents];
+    SPH_CUDA(cudaEventSynchronize(ev[kPhaseEvents - 1]), "cudaEventSynchronize");
+    for (int k = 0; k < 5; ++k) {
+      float ms = 0.0f;
+      SPH_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]), "cudaEventElapsedTime");
+      out[k] += ms;
+    }
+  }
+  return SPH_OK;
+}
+
+void Engine::ReleaseGraphs() {
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+int Engine::Step(int substeps, cudaStream_t st) {
+  if (substeps < 1 || substeps > kMaxSubsteps)
+    return Fail(SPH_ERR_INVALID, "substeps must be in [1, 64]");
+  if (debug_ && substeps != 1)
+    return Fail(SPH_ERR_STATE, "debug capture needs substeps == 1");
+  int rc = BuildLayout(st);
+  if (rc != SPH_OK) return rc;
+  rc = UploadScenes(substeps, st);
+  if (rc != SPH_OK) return rc;
+  if (total_ == 0) return SPH_OK;
+  const bool steady = n_tiles_old_ == n_tiles_new_ && !layout_dirty_;
+  if (use_graphs_ && steady && !debug_) {
+    const auto key = std::make_pair(substeps, cur_);
+    auto it = graphs_.find(key);
+    if (it == graphs_.end()) {
+      cudaGraph_t g = nullptr;
+      SPH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal),
+               "cudaStreamBeginCapture");
+      rc = RunSubsteps(substeps, st);
+      const cudaError_t e = cudaStreamEndCapture(st, &g);
+      if (rc != SPH_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      SPH_CUDA(e, "cudaStreamEndCapture");
+      cudaGraphExec_t ex = nullptr;
+      const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      SPH_CUDA(ei, "cudaGraphInstantiate");
+      it = graphs_.emplace(key, ex).first;
+    }
+    SPH_CUDA(cudaGraphLaunch(it->second, st), "cudaGraphLaunch");
+  } else {
+    rc = RunSubsteps(substeps, st);
+    if (rc != SPH_OK) return rc;
+  }
+  launches_ += static_cast<uint64_t>(kKernelsPredict) +
+               static_cast<uint64_t>(kKernelsPerSubstep) * substeps;
+  profiled_substeps_ = profile_ ? substeps : 0;
+  if (substeps & 1) cur_ = 1 - cur_;
+  if (layout_dirty_ || n_tiles_old_ != n_tiles_new_) {
+    // The data now sits in the compacted layout.
+    if (n_tiles_new_)
+      SPH_CUDA(cudaMemcpyAsync(d_tiles_old_, d_tiles_new_, sizeof(uint2) * n_tiles_new_,
+                               cudaMemcpyDeviceToDevice, st), "tile copy");
+    n_tiles_old_ = n_tiles_new_;
+    for (uint32_t s = 0; s < max_scenes_; ++s)
+      if (scenes_[s].live) old_base_[s] = scenes_[s].base;
+    layout_total_ = total_;
+    layout_dirty_ = false;
+    for (auto& sc : scenes_)
+      if (sc.used && !sc.live) sc.used = false;
+  }
+  debug_valid_ = debug_;
+  return SPH_OK;
+}
+
+int Engine::Download(uint32_t id, float* pos3, float* vel3, float* dens2,
+                     bool device_ptrs, cudaStream_t st) {
+  if (id >= max_scenes_ || !scenes_[id].live)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  const uint32_t n = scenes_[id].n;
+  const uint32_t b = old_base_[id];
+  float *op = pos3, *ov = vel3, *od = dens2;
+  float* scratch = reinterpret_cast<float*>(ctx_.tmp);  // 8n bytes
+  float* scratch_v = reinterpret_cast<float*>(ctx_.keyrank);
+  float* scratch_d = reinterpret_cast<float*>(ctx_.dens_b);
+  if (!device_ptrs) {
+    // tmp/keyrank (8 B per slot each) are too small for 12 B per particle:
+    // use the float4 prediction / post-pressure buffers instead.
+    scratch = reinterpret_cast<float*>(ctx_.pred);
+    scratch_v = reinterpret_cast<float*>(ctx_.velp);
+    op = pos3 ? scratch : nullptr;
+    ov = vel3 ? scratch_v : nullptr;
+    od = dens2 ? scratch_d : nullptr;
+  }
+  SPH_CUDA(launch_export(b, n, d_pos_[cur_], d_vel_[cur_], ctx_.dens_a, op, ov,
+                         od, nullptr, st), "export kernel");
+  if (!device_ptrs) {
+    if (pos3)
+      SPH_CUDA(cudaMemcpyAsync(pos3, scratch, sizeof(float) * 3 * n,
+                               cudaMemcpyDeviceToHost, st), "download positions");
+    if (vel3)
+      SPH_CUDA(cudaMemcpyAsync(vel3, scratch_v, sizeof(float) * 3 * n,
+                               cudaMemcpyDeviceToHost, st), "download velocities");
+    if (dens2)
+      SPH_CUDA(cudaMemcpyAsync(dens2, scratch_d, sizeof(float) * 2 * n,
+                               cudaMemcpyDeviceToHost, st), "download densities");
+  }
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  return SPH_OK;
+}
+
+int Engine::OutPositions(uint32_t id, void** dev_float4) {
+  if (id >= max_scenes_ || !scenes_[id].live || !dev_float4)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  *dev_float4 = d_out4_ + old_base_[id];
+  return SPH_OK;
+}
+
+int Engine::DebugEnable(bool on) {
+  if (on && !d_dbg_hash_) {
+    const uint64_t C = capacity_;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+    chk(Alloc(&d_dbg_hash_, C));
+    chk(Alloc(&d_dbg_key_, C));
+    chk(Alloc(&d_dbg_accp_, C));
+    chk(Alloc(&d_dbg_velv_, C));
+    chk(Alloc(&d_dbg_velp_, C));
+    chk(Alloc(&d_dbg_start_, C + 1));
+    // hash 4 + key 4 + three float3 (36) per particle
+    chk(cudaMalloc(&d_dbg_scratch_, C * 44 + 64));
+    if (e != cudaSuccess) return CudaFail(e, "debug buffers");
+  }
+  if (debug_ != on) ReleaseGraphs();
+  debug_ = on;
+  debug_valid_ = false;
+  return SPH_OK;
+}
+
+int Engine::DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
+                        uint32_t* sorted_ids, uint32_t* start, float* dens2,
+                        float* accp, float* velp, float* velv,
+                        cudaStream_t st) {
+  if (id >= max_scenes_ || !scenes_[id].live)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  if (!debug_valid_) return Fail(SPH_ERR_STATE, "no captured substep");
+  const uint32_t n = scenes_[id].n;
+  const uint32_t b = old_base_[id];
+  uint8_t* s = static_cast<uint8_t*>(d_dbg_scratch_);
+  uint32_t* sh = reinterpret_cast<uint32_t*>(s);
+  uint32_t* sk = sh + n;
+  float* sa = reinterpret_cast<float*>(sk + n);
+  float* sp = sa + 3 * static_cast<uint64_t>(n);
+  float* sv = sp + 3 * static_cast<uint64_t>(n);
+  SPH_CUDA(launch_export_debug(b, n, d_pos_[cur_], d_dbg_hash_, d_dbg_key_,
+                               d_dbg_accp_, d_dbg_velp_, d_dbg_velv_, sh, sk,
+                               sa, sp, sv, st), "debug export kernel");
+  auto d2h = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    if (!dst) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+  };
+  SPH_CUDA(d2h(hash, sh, 4ull * n), "download");
+  SPH_CUDA(d2h(key, sk, 4ull * n), "download");
+  SPH_CUDA(d2h(accp, sa, 12ull * n), "download");
+  SPH_CUDA(d2h(velp, sp, 12ull * n), "download");
+  SPH_CUDA(d2h(velv, sv, 12ull * n), "download");
+  std::vector<uint32_t> st_raw;
+  if (start) {
+    st_raw.resize(n + 1);
+    SPH_CUDA(cudaMemcpyAsync(st_raw.data(), d_dbg_start_ + b, 4ull * (n + 1),
+                             cudaMemcpyDeviceToHost, st), "download start");
+  }
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  if (sorted_ids) {
+    // ids of the captured layout in slot order (pos.w raw bits)
+    std::vector<float4> p(n);
+    SPH_CUDA(cudaMemcpy(p.data(), d_pos_[cur_] + b, sizeof(float4) * n,
+                        cudaMemcpyDeviceToHost), "download ids");
+    for (uint32_t k = 0; k < n; ++k) {
+      uint32_t bits;
+      std::memcpy(&bits, &p[k].w, 4);
+      sorted_ids[k] = bits;
+    }
+  }
+  if (start) {
+    for (uint32_t k = 0; k < n; ++k)
+      start[k] = st_raw[k + 1] > st_raw[k] ? st_raw[k] - b : 0x7fffffffu;
+  }
+  if (dens2) {
+    float* od = reinterpret_cast<float*>(d_dbg_scratch_);
+    SPH_CUDA(launch_export(b, n, d_pos_[cur_], d_vel_[cur_], ctx_.dens_a, nullptr,
+                           nullptr, od, nullptr, st), "export kernel");
+    SPH_CUDA(cudaMemcpyAsync(dens2, od, 8ull * n, cudaMemcpyDeviceToHost, st),
+             "download densities");
+    SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  }
+  return SPH_OK;
+}
+
+int Engine::Status(uint32_t* flags, cudaStream_t st) {
+  uint32_t v = 0;
+  SPH_CUDA(cudaMemcpyAsync(&v, d_status_, 4, cudaMemcpyDeviceToHost, st), "status");
+  SPH_CUDA(cudaMemsetAsync(d_status_, 0, 4, st), "status reset");
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  if (flags) *flags = v;
+  return SPH_OK;
+}
+
+int Engine::SetTuning(const sph_tuning& t) {
+  if (t.block < 32 || t.block > 1024 || (t.block & 31))
+    return Fail(SPH_ERR_INVALID, "block must be a multiple of 32 in [32, 1024]");
+  if (t.particles_per_warp != 32)
+    return Fail(SPH_ERR_INVALID, "particles_per_warp must be 32");
+  if (t.cell_tile < 0) return Fail(SPH_ERR_INVALID, "cell_tile must be >= 0");
+  if (t.block != tuning_.block || t.particles_per_warp != tuning_.particles_per_warp ||
+      t.cell_tile != tuning_.cell_tile)
+    ReleaseGraphs();
+  tuning_ = t;
+  return SPH_OK;
+}
+
+int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
+                     float* best_ms, cudaStream_t st) {
+  if (steps_per_trial < 1) return Fail(SPH_ERR_INVALID, "steps_per_trial >= 1");
+  const int blocks[] = {64, 128, 256, 512};
+  sph_tuning win = tuning_;
+  float win_ms = std::numeric_limits<float>::infinity();
+  cudaEvent_t e0, e1;
+  SPH_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
+  SPH_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+  int rc = SPH_OK;
+  for (int b : blocks) {
+    sph_tuning t{b, 0, 32};
+    if ((rc = SetTuning(t)) != SPH_OK) break;
+    if ((rc = Step(substeps, st)) != SPH_OK) break;  // warm-up + capture
+    cudaEventRecord(e0, st);
+    for (int k = 0; k < steps_per_trial && rc == SPH_OK; ++k) rc = Step(substeps, st);
+    cudaEventRecord(e1, st);
+    if (rc != SPH_OK) break;
+    cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= static_cast<float>(steps_per_trial);
+    if (ms < win_ms) { win_ms = ms; win = t; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != SPH_OK) return rc;
+  rc = SetTuning(win);
+  if (best) *best = win;
+  if (best_ms) *best_ms = win_ms;
+  return rc;
+}
+
+}  // namespace sph

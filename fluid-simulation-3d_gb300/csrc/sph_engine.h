@@ -1,0 +1,132 @@
+// Host-side engine: owns the device buffers of one or more scenes, keeps the
+// layout bookkeeping (which slots each scene occupies), builds the tile tables
+// of the segmented launches and runs the substep pipeline, optionally from a
+// captured CUDA graph.
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sph_gb300.h"
+#include "sph_kernels.h"
+
+namespace sph {
+
+class Engine {
+ public:
+  Engine(uint64_t capacity, uint32_t max_scenes);
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  int Init();  // allocate device memory; SPH_OK or an error code
+
+  int AddScene(const sph_params& p, uint32_t n, const float* pos3,
+               const float* vel3, bool device_ptrs, float dt, uint32_t* id,
+               cudaStream_t st);
+  int RemoveScene(uint32_t id);
+  int SetParams(uint32_t id, const sph_params& p);
+  int GetParams(uint32_t id, sph_params* p) const;
+  int SetDt(uint32_t id, float dt);
+  int Load(uint32_t id, const float* pos3, const float* vel3, bool device_ptrs,
+           cudaStream_t st);
+  int Step(int substeps, cudaStream_t st);
+  int Download(uint32_t id, float* pos3, float* vel3, float* dens2,
+               bool device_ptrs, cudaStream_t st);
+  int OutPositions(uint32_t id, void** dev_float4);
+  int DebugEnable(bool on);
+  int DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
+                  uint32_t* sorted_ids, uint32_t* start, float* dens2,
+                  float* accp, float* velp, float* velv, cudaStream_t st);
+  int Status(uint32_t* flags, cudaStream_t st);
+
+  int SetTuning(const sph_tuning& t);
+  sph_tuning Tuning() const { return tuning_; }
+  int Autotune(int substeps, int steps_per_trial, sph_tuning* best,
+               float* best_ms, cudaStream_t st);
+
+  // Per-phase device timing of each step (CUDA events on the launching
+  // stream, also inside captured graphs).
+  int ProfileEnable(bool on);
+  int PhaseTimes(double out_ms[6]);
+  uint64_t KernelLaunches() const { return launches_; }
+
+  void UseGraphs(bool on) { use_graphs_ = on; }
+  uint32_t NumScenes() const;
+  uint64_t NumParticles() const;
+  uint32_t SceneSize(uint32_t id) const;
+  const char* LastError() const { return err_.c_str(); }
+  int Fail(int code, const std::string& msg);
+  int CudaFail(cudaError_t e, const char* what);
+
+ private:
+  struct Scene {
+    bool used = false;
+    bool live = false;
+    sph_params prm{};
+    uint32_t n = 0;
+    uint32_t base = 0;      // slots in the current layout
+    float dt = 1.0f / 60.0f;
+  };
+  int BuildLayout(cudaStream_t st);
+  int UploadScenes(int substeps, cudaStream_t st);
+  int RunSubsteps(int substeps, cudaStream_t st);
+  void BuildTiles(std::vector<uint2>& out, bool old_layout) const;
+  void ReleaseGraphs();
+
+  uint64_t capacity_;
+  uint32_t max_scenes_;
+  std::vector<Scene> scenes_;
+  std::vector<uint32_t> old_base_;  // per scene: base in the layout a step reads
+  uint64_t layout_total_ = 0;       // slots occupied in the current layout
+  uint32_t total_ = 0;              // live particles (table length)
+  bool layout_dirty_ = true;
+  bool scenes_dirty_ = true;
+  int uploaded_substeps_ = -1;
+
+  // device memory
+  void* arena_ = nullptr;
+  SceneDev* d_scenes_ = nullptr;
+  uint2* d_tiles_old_ = nullptr;
+  uint2* d_tiles_new_ = nullptr;
+  uint32_t n_tiles_old_ = 0, n_tiles_new_ = 0;
+  float4 *d_pos_[2] = {nullptr, nullptr}, *d_vel_[2] = {nullptr, nullptr};
+  int cur_ = 0;  // index of the state buffers holding the current layout
+  LaunchCtx ctx_{};
+  float4* d_out4_ = nullptr;
+  uint32_t* d_status_ = nullptr;
+
+  // debug capture
+  bool debug_ = false;
+  bool debug_valid_ = false;
+  uint32_t* d_dbg_hash_ = nullptr;
+  uint32_t* d_dbg_key_ = nullptr;
+  float4* d_dbg_accp_ = nullptr;
+  float4* d_dbg_velv_ = nullptr;
+  float4* d_dbg_velp_ = nullptr;
+  uint32_t* d_dbg_start_ = nullptr;
+  void* d_dbg_scratch_ = nullptr;
+
+  sph_tuning tuning_{128, 0, 32};
+  int sm_count_ = 0;
+
+  // CUDA graphs, keyed by (substeps, state parity)
+  bool use_graphs_ = true;
+  std::map<std::pair<int, int>, cudaGraphExec_t> graphs_;
+
+  // profiling: kPhaseEvents events per substep, kMaxSubsteps substeps
+  static constexpr int kPhaseEvents = 6;
+  static constexpr int kMaxSubsteps = 64;
+  bool profile_ = false;
+  int profiled_substeps_ = 0;
+  std::vector<cudaEvent_t> prof_ev_;
+  uint64_t launches_ = 0;
+
+  std::string err_;
+};
+
+}  // namespace sph

@@ -1,0 +1,109 @@
+// Host-visible declarations of the SPH kernels' launchers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sph_device.cuh"
+
+namespace sph {
+
+constexpr uint32_t kStatusNonFinite = 0x1u;
+constexpr uint32_t kStatusRange = 0x2u;
+
+// A tile is (scene | (len-1) << 27, first slot): up to 32 consecutive slots
+// of one scene.
+constexpr uint32_t kTileSceneBits = 27;
+__host__ __device__ __forceinline__ uint32_t tile_scene(uint2 t) {
+  return t.x & ((1u << kTileSceneBits) - 1u);
+}
+__host__ __device__ __forceinline__ uint32_t tile_len(uint2 t) {
+  return (t.x >> kTileSceneBits) + 1u;
+}
+__host__ __device__ __forceinline__ uint2 make_tile(uint32_t scene,
+                                                    uint32_t first,
+                                                    uint32_t len) {
+  return make_uint2(scene | ((len - 1u) << kTileSceneBits), first);
+}
+
+// glm::sign for floats: 1, -1, or 0 for +-0 and NaN.
+__device__ __forceinline__ float copysign_or_zero(float x) {
+  return static_cast<float>(0.0f < x) - static_cast<float>(x < 0.0f);
+}
+
+struct Tiles {
+  const uint2* d = nullptr;  // device tile table
+  uint32_t n = 0;
+};
+
+// Device buffers and launch shape used by one engine.
+struct LaunchCtx {
+  const SceneDev* scenes = nullptr;
+  float4* pos = nullptr;   // state A (read at substep start)
+  float4* vel = nullptr;
+  float4* pos2 = nullptr;  // state B (written by the reorder)
+  float4* vel2 = nullptr;
+  float4* pred = nullptr;
+  float4* velp = nullptr;
+  float2* dens_a = nullptr;
+  float4* dens_b = nullptr;
+  uint2* keyrank = nullptr;
+  uint2* tmp = nullptr;
+  uint32_t* count = nullptr;
+  uint32_t* start = nullptr;
+  uint32_t* partial = nullptr;
+  float4* out4 = nullptr;
+  uint32_t* status = nullptr;
+  uint32_t* dbg_hash = nullptr;
+  uint32_t* dbg_key = nullptr;
+  float4* dbg_accp = nullptr;
+  float4* dbg_velv = nullptr;
+  uint32_t src_limit = 0;  // slots of the layout a substep reads
+  int block_misc = 256;   // predict/scatter/reorder
+  int block_nbr = 128;    // neighbour kernels
+  uint32_t max_blocks = 0;  // persistent grid cap (0 = no cap)
+};
+
+inline uint32_t grid_for(uint32_t ntiles, int block, uint32_t max_blocks) {
+  const uint32_t wpb = static_cast<uint32_t>(block) / 32u;
+  uint32_t g = (ntiles + wpb - 1) / wpb;
+  if (max_blocks && g > max_blocks) g = max_blocks;
+  return g == 0 ? 1 : g;
+}
+
+uint32_t scan_partials_needed(uint64_t len);
+
+cudaError_t launch_predict_hash(const LaunchCtx& c, const Tiles& old_tiles,
+                                cudaStream_t st);
+cudaError_t launch_scan(const LaunchCtx& c, uint32_t len, cudaStream_t st);
+cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
+                                const Tiles& new_tiles, uint32_t total,
+                                cudaStream_t st);
+cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
+                           cudaStream_t st);
+cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
+                            cudaStream_t st);
+cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
+                                  int fuse_next, int write_out,
+                                  cudaStream_t st);
+
+// Kernels launched by one substep (scan 3, scatter, reorder, density,
+// pressure, viscosity) and by the standalone prediction of a step's first
+// substep.
+constexpr int kKernelsPerSubstep = 8;
+constexpr int kKernelsPredict = 1;
+cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
+                          const float4* vel, const float2* dens, float* opos,
+                          float* ovel, float* odens, uint32_t* oids,
+                          cudaStream_t st);
+cudaError_t launch_export_debug(uint32_t first, uint32_t n, const float4* pos,
+                                const uint32_t* dhash, const uint32_t* dkey,
+                                const float4* accp, const float4* velp,
+                                const float4* velv, uint32_t* ohash,
+                                uint32_t* okey, float* oaccp, float* ovelp,
+                                float* ovelv, cudaStream_t st);
+cudaError_t launch_import(uint32_t first, uint32_t n, const float* ipos,
+                          const float* ivel, float4* pos, float4* vel,
+                          cudaStream_t st);
+
+}  // namespace sph

@@ -1,0 +1,208 @@
+/*
+ * sph_gb300 -- C ABI of the GB300 (sm_103a) SPH substep library.
+ *
+ * Drop-in for the per-substep SPH pipeline of Allkams/Fluid-Simulation-3D
+ * (engine/physics/physicsWorld.cc): spatial-hash build, density and near
+ * density, pressure + near pressure + viscosity, integrate with box
+ * collision. The library owns all device memory; host pointers passed in are
+ * caller-owned and only read/written during the call. Every call returns an
+ * int status (SPH_OK = 0); sph_last_error() gives the message of the last
+ * failure on a handle. A handle is used from one host thread and enqueues its
+ * work on the caller's CUDA stream (passed as a plain pointer, NULL = the
+ * legacy default stream). There is no CPU fallback: without a usable CUDA
+ * device every compute call returns SPH_ERR_CUDA.
+ *
+ * Particle arrays on the host side are AoS float[3*n] in the caller's
+ * particle order (the reference's `positions` / `velocity` index order,
+ * physicsWorld.h:79,119).
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_OK 0
+#define SPH_ERR_INVALID -1   /* bad argument or size                      */
+#define SPH_ERR_CUDA -2      /* CUDA runtime error / no device            */
+#define SPH_ERR_NOMEM -3     /* device allocation or budget exhausted     */
+#define SPH_ERR_STATE -4     /* call not valid in the handle's state      */
+#define SPH_ERR_DEVICE -5    /* a kernel raised a device status flag      */
+
+/* Device status flags (sph_status). */
+#define SPH_STATUS_NONFINITE 0x1u  /* a position/velocity became NaN/inf   */
+#define SPH_STATUS_RANGE 0x2u      /* an index fell outside its buffer     */
+
+/* Settings surface of Physics::Fluid::FluidSimulation
+ * (engine/physics/physicsWorld.h:96-106,145) plus the two constants the
+ * reference hard-codes: collision damping 0.95 (physicsWorld.cc:87) and the
+ * 1/120 s prediction look-ahead (physicsWorld.cc:47). */
+typedef struct sph_params {
+  float radius;             /* interactionRadius,  default 0.35          */
+  float cutoff_sq;          /* sqrRadius, default 0.35f*0.35f (the
+                               reference never updates it, :234-237)     */
+  float target_density;     /* TargetDensity,      default 99.7          */
+  float pressure_mult;      /* pressureMultiplier, default 300           */
+  float near_pressure_mult; /* nearPressureMultiplier, default 20        */
+  float viscosity;          /* viscosityStrength,  default 0.5           */
+  float gravity_scale;      /* gravityScale,       default 10            */
+  int32_t gravity_on;       /* gravity,            default 0 (off)       */
+  float bound[3];           /* BoundScale,         default 20,20,20      */
+  float damping;            /* collision damping,  default 0.95          */
+  float predict_dt;         /* prediction look-ahead, default 1/120      */
+} sph_params;
+
+typedef struct sph_sim sph_sim;
+
+/* Reference defaults of physicsWorld.h:96-106,145 and physicsWorld.cc:47,87. */
+void sph_default_params(sph_params *out);
+
+/* Create a single-scene simulation of n particles (replaces
+ * FluidSimulation::getInstance + InitializeData, physicsWorld.cc:32-37,
+ * 112-147; the lattice layout is left to the caller: state is zero until
+ * sph_upload). n must be in [1, 2^24) -- the reference stores particle
+ * indices as floats (physicsWorld.h:128). */
+int sph_create(const sph_params *params, uint32_t n, sph_sim **out);
+int sph_destroy(sph_sim *sim);
+
+/* Settings setters/getters (physicsWorld.cc:214-302). Take effect at the
+ * next sph_step. */
+int sph_set_params(sph_sim *sim, const sph_params *params);
+int sph_get_params(const sph_sim *sim, sph_params *out);
+uint32_t sph_num_particles(const sph_sim *sim);
+
+/* Load positions / velocities (host, float[3n]; vel may be NULL = zero).
+ * Replaces writing the public `positions` buffer (physicsWorld.h:79). */
+int sph_upload(sph_sim *sim, const float *pos3, const float *vel3,
+               void *stream);
+
+/* Advance by dt split into `substeps` equal substeps: each substep is one
+ * reference FluidSimulation::Update(dt / substeps) (physicsWorld.cc:39-111)
+ * with Jacobi viscosity (every particle reads the post-pressure velocity
+ * snapshot). Asynchronous on `stream`. */
+int sph_step(sph_sim *sim, float dt, int substeps, void *stream);
+
+/* Read back state in the caller's particle order (host pointers; any may be
+ * NULL): pos3/vel3 float[3n], dens2 float[2n] (density, near density of the
+ * last substep, getDensity/getNearDensity physicsWorld.cc:161-170).
+ * Synchronises `stream`. */
+int sph_download(sph_sim *sim, float *pos3, float *vel3, float *dens2,
+                 void *stream);
+
+/* Device pointer to the headless OutPositions buffer (physicsWorld.h:80):
+ * float4[n] = (position, 0.34) in the caller's order, refreshed by every
+ * sph_step. Valid until sph_destroy. */
+int sph_out_positions(sph_sim *sim, void **dev_float4);
+
+/* Same as sph_step/sph_upload/sph_download but with device pointers
+ * (float[3n] on the handle's device) -- no host copies. */
+int sph_upload_device(sph_sim *sim, const float *dpos3, const float *dvel3,
+                      void *stream);
+int sph_download_device(sph_sim *sim, float *dpos3, float *dvel3,
+                        float *ddens2, void *stream);
+
+/* Parity capture: when enabled, the FIRST substep of the next sph_step
+ * records the intermediates of the reference's phases. sph_debug_export then
+ * returns them (host pointers, any may be NULL):
+ *   hash[n], key[n]    -- HashCell / GetKeyFromHash of each particle
+ *                         (physicsWorld.cc:505-516), caller order;
+ *   sorted_ids[n]      -- spatialLookup order, canonical (key, index);
+ *   start[n]           -- startIndices (0x7fffffff = empty key);
+ *   dens2[2n]          -- density, near density;
+ *   acc_p3[3n]         -- pressureForce / density (physicsWorld.cc:421);
+ *   vel_p3[3n]         -- velocity after the pressure pass;
+ *   vel_v3[3n]         -- velocity after the viscosity pass (pre-collision).
+ * Synchronises `stream`. */
+int sph_debug_enable(sph_sim *sim, int enable);
+int sph_debug_export(sph_sim *sim, uint32_t *hash, uint32_t *key,
+                     uint32_t *sorted_ids, uint32_t *start, float *dens2,
+                     float *acc_p3, float *vel_p3, float *vel_v3,
+                     void *stream);
+
+/* Device status flags OR-ed by kernels since the last call (cleared by the
+ * read). Synchronises `stream`. */
+int sph_status(sph_sim *sim, uint32_t *flags, void *stream);
+
+/* Per-phase device timing (replaces getElapsedTime{Gravity,Spatial,Density,
+ * Pressure,Viscosity,PosNColl}, physicsWorld.h:45-50, whose values are
+ * host-clock ms of the last Update). When enabled, every sph_step records
+ * CUDA events on its stream between the phases; sph_phase_times returns the
+ * last step's ms per phase summed over its substeps, in that order
+ * (integration runs inside the viscosity kernel, so PosNColl is 0).
+ * Synchronises on the last event. */
+int sph_profile_enable(sph_sim *sim, int enable);
+int sph_phase_times(sph_sim *sim, double out_ms[6]);
+
+/* Number of this library's kernels the handle has launched so far
+ * (including those replayed from captured graphs). */
+uint64_t sph_kernel_launches(const sph_sim *sim);
+
+/* Message of the last failed call on this handle ("" if none). */
+const char *sph_last_error(const sph_sim *sim);
+
+/* Message of the last failed sph_create / batch create (no handle yet). */
+const char *sph_global_error(void);
+
+/* ------------------------------------------------------------------------
+ * Batched form: many independent scenes of uneven sizes advanced together.
+ * Each kernel of a substep is one segmented, persistent launch over all
+ * scenes; a whole step is captured once in a CUDA graph and replayed.
+ * Scenes keep their own settings, table (key = hash % n_scene) and dt.
+ * ---------------------------------------------------------------------- */
+typedef struct sph_batch sph_batch;
+
+/* capacity: total particles resident at once (device memory is sized for
+ * it); max_scenes: scene slots. */
+int sph_batch_create(uint64_t capacity, uint32_t max_scenes, sph_batch **out);
+int sph_batch_destroy(sph_batch *b);
+
+/* Add a scene (host arrays float[3n]; vel may be NULL). Becomes part of the
+ * next sph_batch_step. Returns its id in *scene_id. Fails with SPH_ERR_NOMEM
+ * when it does not fit the capacity. */
+int sph_batch_add(sph_batch *b, const sph_params *params, uint32_t n,
+                  const float *pos3, const float *vel3, float dt,
+                  uint32_t *scene_id, void *stream);
+
+/* Remove a scene (its slot and particles are released at the next step). */
+int sph_batch_remove(sph_batch *b, uint32_t scene_id);
+
+/* Advance every resident scene by one step of `substeps` substeps of its own
+ * dt / substeps. */
+int sph_batch_step(sph_batch *b, int substeps, void *stream);
+
+/* Read one scene back (host pointers, caller order, any may be NULL).
+ * Synchronises `stream`. */
+int sph_batch_download(sph_batch *b, uint32_t scene_id, float *pos3,
+                       float *vel3, float *dens2, void *stream);
+
+/* Launch configuration of the neighbour kernels and the autotuner that picks
+ * it by timing the current scene set (block size, cell-tile size and
+ * particles per warp; see sph_tuning). */
+typedef struct sph_tuning {
+  int32_t block;           /* threads per block of the neighbour kernels */
+  int32_t cell_tile;       /* candidate slots staged per tile             */
+  int32_t particles_per_warp; /* 32 = one particle per lane; 8/16 = lanes
+                                 split each particle's candidates         */
+} sph_tuning;
+int sph_batch_set_tuning(sph_batch *b, const sph_tuning *t);
+int sph_batch_get_tuning(const sph_batch *b, sph_tuning *t);
+/* Sweep the tuning space on the resident scenes (runs real steps, so the
+ * state advances by `steps_per_trial` steps per candidate), keep the fastest
+ * and report it in *best (may be NULL) and its ms per step in *best_ms. */
+int sph_batch_autotune(sph_batch *b, int substeps, int steps_per_trial,
+                       sph_tuning *best, float *best_ms, void *stream);
+
+uint32_t sph_batch_num_scenes(const sph_batch *b);
+uint64_t sph_batch_num_particles(const sph_batch *b);
+uint64_t sph_batch_kernel_launches(const sph_batch *b);
+int sph_batch_profile_enable(sph_batch *b, int enable);
+int sph_batch_phase_times(sph_batch *b, double out_ms[6]);
+const char *sph_batch_last_error(const sph_batch *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
