@@ -76,6 +76,9 @@ Engine::~Engine() {
   ReleaseGraphs();
   for (auto& e : prof_ev_)
     if (e) cudaEventDestroy(e);
+  if (join_in_) cudaEventDestroy(join_in_);
+  if (join_out_) cudaEventDestroy(join_out_);
+  if (work_) cudaStreamDestroy(work_);
   void* ptrs[] = {d_scenes_, d_tiles_old_, d_tiles_new_, d_pos_[0], d_pos_[1],
                   d_vel_[0], d_vel_[1], ctx_.pred, ctx_.velp, ctx_.dens_a,
                   ctx_.dens_b, ctx_.keyrank, ctx_.tmp, ctx_.count, ctx_.start,
@@ -110,6 +113,12 @@ int Engine::Init() {
   SPH_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
   SPH_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, dev),
            "cudaDeviceGetAttribute");
+  SPH_CUDA(cudaStreamCreateWithFlags(&work_, cudaStreamNonBlocking),
+           "cudaStreamCreateWithFlags");
+  SPH_CUDA(cudaEventCreateWithFlags(&join_in_, cudaEventDisableTiming),
+           "cudaEventCreate");
+  SPH_CUDA(cudaEventCreateWithFlags(&join_out_, cudaEventDisableTiming),
+           "cudaEventCreate");
   const uint64_t C = capacity_;
   const uint64_t max_tiles = C / kTile + max_scenes_ + 1;
   cudaError_t e = cudaSuccess;
@@ -329,6 +338,9 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
   int cur = cur_;
   const Tiles told{d_tiles_old_, n_tiles_old_};
   const Tiles tnew{d_tiles_new_, n_tiles_new_};
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  SPH_CUDA(cudaStreamIsCapturing(st, &cap), "cudaStreamIsCapturing");
+  const bool capturing = cap == cudaStreamCaptureStatusActive;
   for (int ss = 0; ss < substeps; ++ss) {
     c.pos = d_pos_[cur];
     c.vel = d_vel_[cur];
@@ -342,8 +354,12 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
     const Tiles& first = ss == 0 ? told : tnew;
     cudaEvent_t* ev = profile_ ? &prof_ev_[ss * kPhaseEvents] : nullptr;
     cudaError_t e = cudaSuccess;
+    // External records become event nodes when the stream is being captured
+    // (a plain record would only express a dependency).
     auto mark = [&](int k) {
-      if (ev && e == cudaSuccess) e = cudaEventRecord(ev[k], st);
+      if (!ev || e != cudaSuccess) return;
+      e = capturing ? cudaEventRecordWithFlags(ev[k], st, cudaEventRecordExternal)
+                    : cudaEventRecord(ev[k], st);
     };
     mark(0);
     if (ss == 0) e = launch_predict_hash(c, first, st);
@@ -417,37 +433,44 @@ int Engine::Step(int substeps, cudaStream_t st) {
   if (rc != SPH_OK) return rc;
   rc = UploadScenes(substeps, st);
   if (rc != SPH_OK) return rc;
-  if (total_ == 0) return SPH_OK;
-  const bool steady = n_tiles_old_ == n_tiles_new_ && !layout_dirty_;
-  if (use_graphs_ && steady && !debug_) {
-    const auto key = std::make_pair(substeps, cur_);
-    auto it = graphs_.find(key);
-    if (it == graphs_.end()) {
-      cudaGraph_t g = nullptr;
-      SPH_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal),
-               "cudaStreamBeginCapture");
-      rc = RunSubsteps(substeps, st);
-      const cudaError_t e = cudaStreamEndCapture(st, &g);
-      if (rc != SPH_OK) {
-        if (g) cudaGraphDestroy(g);
-        return rc;
+  if (total_ > 0) {
+    // join: the work stream starts after everything queued on `st`
+    SPH_CUDA(cudaEventRecord(join_in_, st), "cudaEventRecord");
+    SPH_CUDA(cudaStreamWaitEvent(work_, join_in_, 0), "cudaStreamWaitEvent");
+    const bool steady = n_tiles_old_ == n_tiles_new_ && !layout_dirty_;
+    if (use_graphs_ && steady && !debug_) {
+      const auto key = std::make_pair(substeps, cur_);
+      auto it = graphs_.find(key);
+      if (it == graphs_.end()) {
+        cudaGraph_t g = nullptr;
+        SPH_CUDA(cudaStreamBeginCapture(work_, cudaStreamCaptureModeThreadLocal),
+                 "cudaStreamBeginCapture");
+        rc = RunSubsteps(substeps, work_);
+        const cudaError_t e = cudaStreamEndCapture(work_, &g);
+        if (rc != SPH_OK) {
+          if (g) cudaGraphDestroy(g);
+          return rc;
+        }
+        SPH_CUDA(e, "cudaStreamEndCapture");
+        cudaGraphExec_t ex = nullptr;
+        const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        SPH_CUDA(ei, "cudaGraphInstantiate");
+        it = graphs_.emplace(key, ex).first;
       }
-      SPH_CUDA(e, "cudaStreamEndCapture");
-      cudaGraphExec_t ex = nullptr;
-      const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
-      cudaGraphDestroy(g);
-      SPH_CUDA(ei, "cudaGraphInstantiate");
-      it = graphs_.emplace(key, ex).first;
+      SPH_CUDA(cudaGraphLaunch(it->second, work_), "cudaGraphLaunch");
+    } else {
+      rc = RunSubsteps(substeps, work_);
+      if (rc != SPH_OK) return rc;
     }
-    SPH_CUDA(cudaGraphLaunch(it->second, st), "cudaGraphLaunch");
-  } else {
-    rc = RunSubsteps(substeps, st);
-    if (rc != SPH_OK) return rc;
+    // join back: later work on `st` sees the step's results
+    SPH_CUDA(cudaEventRecord(join_out_, work_), "cudaEventRecord");
+    SPH_CUDA(cudaStreamWaitEvent(st, join_out_, 0), "cudaStreamWaitEvent");
+    launches_ += static_cast<uint64_t>(kKernelsPredict) +
+                 static_cast<uint64_t>(kKernelsPerSubstep) * substeps;
+    profiled_substeps_ = profile_ ? substeps : 0;
+    if (substeps & 1) cur_ = 1 - cur_;
   }
-  launches_ += static_cast<uint64_t>(kKernelsPredict) +
-               static_cast<uint64_t>(kKernelsPerSubstep) * substeps;
-  profiled_substeps_ = profile_ ? substeps : 0;
-  if (substeps & 1) cur_ = 1 - cur_;
   if (layout_dirty_ || n_tiles_old_ != n_tiles_new_) {
     // The data now sits in the compacted layout.
     if (n_tiles_new_)

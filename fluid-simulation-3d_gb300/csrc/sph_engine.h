@@ -114,6 +114,12 @@ class Engine {
   sph_tuning tuning_{128, 0, 32};
   int sm_count_ = 0;
 
+  // The substep pipeline runs on an engine-owned non-blocking stream (stream
+  // capture is not allowed on the legacy default stream), joined to the
+  // caller's stream by events before and after each step.
+  cudaStream_t work_ = nullptr;
+  cudaEvent_t join_in_ = nullptr, join_out_ = nullptr;
+
   // CUDA graphs, keyed by (substeps, state parity)
   bool use_graphs_ = true;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs_;

@@ -41,6 +41,13 @@ __device__ __forceinline__ uint32_t warps_total() {
   return gridDim.x * (blockDim.x >> 5);
 }
 
+// glm dot(v, v) of physicsWorld.cc:355: three rounded products summed left to
+// right (no FMA contraction), so boundary pairs classify as in the reference.
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                   __fmul_rn(dz, dz));
+}
+
 __device__ __forceinline__ void flag(uint32_t* status, uint32_t f) {
   atomicOr(status, f);
 }
@@ -275,10 +282,9 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
     float s2 = 0.0f, s3 = 0.0f;
     walk27(S, start, pred, p, [&](uint32_t, float4 q) {
       const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-      const float d2 = dx * dx + dy * dy + dz * dz;
+      const float d2 = dist2(dx, dy, dz);
       if (d2 <= S.cut_lt) {
-        const float dist = d2 > 0.0f ? d2 * rsqrtf(d2) : 0.0f;
-        const float w = S.r - dist;
+        const float w = S.r - __fsqrt_rn(d2);
         const float w2 = w * w;
         s2 += w2;
         s3 += w2 * w;
@@ -319,11 +325,11 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
     walk27(S, start, pred, p, [&](uint32_t j, float4 q) {
       if (j == i) return;
       const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-      const float d2 = dx * dx + dy * dy + dz * dz;
+      const float d2 = dist2(dx, dy, dz);
       if (d2 <= S.cut_le) {
         const float4 b = __ldg(dens_b + j);
+        const float dist = __fsqrt_rn(d2);
         const float inv = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
-        const float dist = d2 * inv;
         const float w = S.r - dist;
         const float a2 = S.ds2h * fmaf(Pi, b.x, b.y);
         const float a3 = S.ds3h * w * fmaf(Pni, b.z, b.w);
@@ -372,9 +378,10 @@ __global__ void k_visc_integrate(
       walk27(S, start, pred, p, [&](uint32_t j, float4 q) {
         if (j == i) return;
         const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float d2 = dist2(dx, dy, dz);
         if (d2 <= S.cut_lt) {
-          const float w = S.r2 - d2;
+          const float dist = __fsqrt_rn(d2);
+          const float w = __fsub_rn(S.r2, __fmul_rn(dist, dist));
           const float w3 = w * w * w;
           const float4 vj = __ldg(velp + j);
           fx += (vj.x - vi.x) * w3;
