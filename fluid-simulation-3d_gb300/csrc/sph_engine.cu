@@ -38,6 +38,7 @@ SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base,
   const float t_le = LargestWith(r, [r](float s) { return s <= r; });
   d.cut_lt = std::min(p.cutoff_sq, t_lt);
   d.cut_le = std::min(p.cutoff_sq, t_le);
+  d.cut_hi = d.cut_le * 1.000002f;
   d.r2 = r * r;
   // kernels.h:28,40,52,64,76 -- same float expressions.
   d.vol2 = 15.0f / (2.0f * kPiF * powf(r, 5.0f));
@@ -81,7 +82,8 @@ Engine::~Engine() {
   if (work_) cudaStreamDestroy(work_);
   void* ptrs[] = {d_scenes_, d_tiles_old_, d_tiles_new_, d_pos_[0], d_pos_[1],
                   d_vel_[0], d_vel_[1], ctx_.pred, ctx_.velp, ctx_.dens_a,
-                  ctx_.dens_b, ctx_.keyrank, ctx_.tmp, ctx_.count, ctx_.start,
+                  ctx_.dens_b, ctx_.keyrank, ctx_.tmp_hi, ctx_.tmp_src, ctx_.hash_s,
+                  ctx_.nbr, ctx_.ncount, ctx_.count, ctx_.start,
                   ctx_.partial, d_out4_, d_status_, d_dbg_hash_, d_dbg_key_,
                   d_dbg_accp_, d_dbg_velv_, d_dbg_velp_, d_dbg_start_,
                   d_dbg_scratch_};
@@ -135,7 +137,11 @@ int Engine::Init() {
   chk(Alloc(&ctx_.dens_a, C));
   chk(Alloc(&ctx_.dens_b, C));
   chk(Alloc(&ctx_.keyrank, C));
-  chk(Alloc(&ctx_.tmp, C));
+  chk(Alloc(&ctx_.tmp_hi, C));
+  chk(Alloc(&ctx_.tmp_src, C));
+  chk(Alloc(&ctx_.hash_s, C));
+  chk(Alloc(&ctx_.ncount, C));
+  chk(Alloc(&ctx_.nbr, C * static_cast<uint64_t>(kNbrCap)));
   chk(Alloc(&ctx_.count, C));
   chk(Alloc(&ctx_.start, C + 1));
   chk(Alloc(&ctx_.partial, scan_partials_needed(C)));
@@ -154,6 +160,9 @@ int Engine::Init() {
   ctx_.scenes = d_scenes_;
   ctx_.out4 = d_out4_;
   ctx_.status = d_status_;
+  ctx_.nbr_stride = static_cast<uint32_t>(C);
+  ctx_.nbr_cap = kNbrCap;
+  SPH_CUDA(density_configure(tuning_.cell_tile), "cudaFuncSetAttribute");
   return SPH_OK;
 }
 
@@ -333,6 +342,7 @@ int Engine::UploadScenes(int substeps, cudaStream_t st) {
 int Engine::RunSubsteps(int substeps, cudaStream_t st) {
   LaunchCtx c = ctx_;
   c.block_nbr = tuning_.block;
+  c.tile_cap = tuning_.cell_tile;
   c.max_blocks = 0;
   c.src_limit = static_cast<uint32_t>(capacity_);
   int cur = cur_;
@@ -347,7 +357,6 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
     c.pos2 = d_pos_[1 - cur];
     c.vel2 = d_vel_[1 - cur];
     const bool dbg = debug_ && ss == 0;
-    c.dbg_hash = dbg ? d_dbg_hash_ : nullptr;
     c.dbg_key = dbg ? d_dbg_key_ : nullptr;
     c.dbg_accp = dbg ? d_dbg_accp_ : nullptr;
     c.dbg_velv = dbg ? d_dbg_velv_ : nullptr;
@@ -370,6 +379,9 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
     if (e == cudaSuccess && dbg) {
       e = cudaMemcpyAsync(d_dbg_start_, c.start, sizeof(uint32_t) * (total_ + 1),
                           cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_dbg_hash_, c.hash_s, sizeof(uint32_t) * total_,
+                            cudaMemcpyDeviceToDevice, st);
     }
     if (e == cudaSuccess) e = launch_density(c, tnew, st);
     mark(3);
@@ -495,14 +507,12 @@ int Engine::Download(uint32_t id, float* pos3, float* vel3, float* dens2,
   const uint32_t n = scenes_[id].n;
   const uint32_t b = old_base_[id];
   float *op = pos3, *ov = vel3, *od = dens2;
-  float* scratch = reinterpret_cast<float*>(ctx_.tmp);  // 8n bytes
-  float* scratch_v = reinterpret_cast<float*>(ctx_.keyrank);
+  // Host copies stage through the prediction / post-pressure / density
+  // buffers (16 B per slot, rewritten by every substep before use).
+  float* scratch = reinterpret_cast<float*>(ctx_.pred);
+  float* scratch_v = reinterpret_cast<float*>(ctx_.velp);
   float* scratch_d = reinterpret_cast<float*>(ctx_.dens_b);
   if (!device_ptrs) {
-    // tmp/keyrank (8 B per slot each) are too small for 12 B per particle:
-    // use the float4 prediction / post-pressure buffers instead.
-    scratch = reinterpret_cast<float*>(ctx_.pred);
-    scratch_v = reinterpret_cast<float*>(ctx_.velp);
     op = pos3 ? scratch : nullptr;
     ov = vel3 ? scratch_v : nullptr;
     od = dens2 ? scratch_d : nullptr;
@@ -579,15 +589,14 @@ int Engine::DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
   SPH_CUDA(d2h(accp, sa, 12ull * n), "download");
   SPH_CUDA(d2h(velp, sp, 12ull * n), "download");
   SPH_CUDA(d2h(velv, sv, 12ull * n), "download");
-  std::vector<uint32_t> st_raw;
-  if (start) {
-    st_raw.resize(n + 1);
-    SPH_CUDA(cudaMemcpyAsync(st_raw.data(), d_dbg_start_ + b, 4ull * (n + 1),
-                             cudaMemcpyDeviceToHost, st), "download start");
-  }
+  std::vector<uint32_t> st_raw(n + 1);
+  SPH_CUDA(cudaMemcpyAsync(st_raw.data(), d_dbg_start_ + b, 4ull * (n + 1),
+                           cudaMemcpyDeviceToHost, st), "download start");
   SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   if (sorted_ids) {
-    // ids of the captured layout in slot order (pos.w raw bits)
+    // ids of the captured layout in slot order (pos.w raw bits), ordered by
+    // (hash, index) inside each key bucket; the reference's lookup order is
+    // (key, index): sort each bucket by index.
     std::vector<float4> p(n);
     SPH_CUDA(cudaMemcpy(p.data(), d_pos_[cur_] + b, sizeof(float4) * n,
                         cudaMemcpyDeviceToHost), "download ids");
@@ -595,6 +604,10 @@ int Engine::DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
       uint32_t bits;
       std::memcpy(&bits, &p[k].w, 4);
       sorted_ids[k] = bits;
+    }
+    for (uint32_t k = 0; k < n; ++k) {
+      const uint32_t s0 = st_raw[k] - b, s1 = st_raw[k + 1] - b;
+      if (s1 > s0 + 1 && s1 <= n) std::sort(sorted_ids + s0, sorted_ids + s1);
     }
   }
   if (start) {
@@ -626,10 +639,14 @@ int Engine::SetTuning(const sph_tuning& t) {
     return Fail(SPH_ERR_INVALID, "block must be a multiple of 32 in [32, 1024]");
   if (t.particles_per_warp != 32)
     return Fail(SPH_ERR_INVALID, "particles_per_warp must be 32");
-  if (t.cell_tile < 0) return Fail(SPH_ERR_INVALID, "cell_tile must be >= 0");
+  // 4 warps per density block share the SM's 227 KB of shared memory
+  if (t.cell_tile < 128 || t.cell_tile > 3456 || (t.cell_tile & 31))
+    return Fail(SPH_ERR_INVALID, "cell_tile must be a multiple of 32 in [128, 3456]");
   if (t.block != tuning_.block || t.particles_per_warp != tuning_.particles_per_warp ||
       t.cell_tile != tuning_.cell_tile)
     ReleaseGraphs();
+  if (t.cell_tile != tuning_.cell_tile)
+    SPH_CUDA(density_configure(t.cell_tile), "cudaFuncSetAttribute");
   tuning_ = t;
   return SPH_OK;
 }
@@ -637,15 +654,16 @@ int Engine::SetTuning(const sph_tuning& t) {
 int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
                      float* best_ms, cudaStream_t st) {
   if (steps_per_trial < 1) return Fail(SPH_ERR_INVALID, "steps_per_trial >= 1");
-  const int blocks[] = {64, 128, 256, 512};
+  std::vector<sph_tuning> space;
+  for (int b : {64, 128, 256, 512})
+    for (int tile : {512, 1024, 2048}) space.push_back(sph_tuning{b, tile, 32});
   sph_tuning win = tuning_;
   float win_ms = std::numeric_limits<float>::infinity();
   cudaEvent_t e0, e1;
   SPH_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
   SPH_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
   int rc = SPH_OK;
-  for (int b : blocks) {
-    sph_tuning t{b, 0, 32};
+  for (const sph_tuning& t : space) {
     if ((rc = SetTuning(t)) != SPH_OK) break;
     if ((rc = Step(substeps, st)) != SPH_OK) break;  // warm-up + capture
     cudaEventRecord(e0, st);

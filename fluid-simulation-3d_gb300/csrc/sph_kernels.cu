@@ -2,25 +2,31 @@
 //
 // One substep (engine/physics/physicsWorld.cc:39-111) is:
 //   k_predict_hash   gravity + prediction + cell hash + key, counting-sort
-//                    histogram (atomic arrival rank)        :42-48, :473-482
+//                    histogram (warp-aggregated atomics)    :42-48, :473-482
 //   k_scan_*         exclusive prefix of the key histogram = start table
-//   k_scatter        bucket each particle at start[key] + rank
-//   k_reorder        canonical (key, index) order inside each bucket and
-//                    gather of the state into SoA float4      :484-496
-//   k_density        density / near density                  :304-365
-//   k_pressure       pressure + near pressure -> velocity     :367-422
-//   k_visc_integrate Jacobi viscosity, integrate, box collision, and the
-//                    next substep's k_predict_hash fused in  :424-464, :81-108
-// Every kernel is a persistent, segmented launch: warps stride over a tile
-// table whose entries are (scene, first slot) runs of 32 particles, so one
+//   k_scatter        bucket each particle at start[key] + arrival rank
+//   k_reorder        deterministic order inside each bucket and gather of
+//                    the state into SoA float4                :484-496
+//   k_density        cell tiles staged in shared memory; density / near
+//                    density and each particle's neighbour list :304-365
+//   k_pressure       pressure + near pressure over the list   :367-422
+//   k_visc_integrate Jacobi viscosity over the list, integrate, box
+//                    collision, next substep's prediction    :424-464, :81-108
+//
+// Inside a key bucket particles are ordered by (cell hash, index): each cell
+// is a contiguous run (the reference orders a bucket only by key; its
+// canonical (key, index) order is rebuilt from this one on export). Every
+// kernel is a persistent, segmented launch: warps stride over a tile table
+// of (scene, first slot) runs of up to 32 particles of one scene, so one
 // launch serves any number of scenes of uneven sizes.
 #include "sph_kernels.h"
-
-#include <cstdio>
 
 namespace sph {
 
 namespace {
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr float kInf = __builtin_huge_valf();
 
 constexpr uint32_t Delta(int o) {
   return static_cast<uint32_t>(o / 9 - 1) * kHashX +
@@ -28,6 +34,9 @@ constexpr uint32_t Delta(int o) {
          static_cast<uint32_t>(o % 3 - 1) * kHashZ;
 }
 
+// hash(c + offset_o) - hash(c) for the 27 offsets of physicsWorld.h:131-143.
+// HashCell is linear modulo 2^32, so the neighbour buckets of a cell depend
+// only on its hash.
 __constant__ uint32_t c_delta[27] = {
     Delta(0),  Delta(1),  Delta(2),  Delta(3),  Delta(4),  Delta(5),  Delta(6),
     Delta(7),  Delta(8),  Delta(9),  Delta(10), Delta(11), Delta(12), Delta(13),
@@ -40,6 +49,7 @@ __device__ __forceinline__ uint32_t warp_id_global() {
 __device__ __forceinline__ uint32_t warps_total() {
   return gridDim.x * (blockDim.x >> 5);
 }
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 
 // glm dot(v, v) of physicsWorld.cc:355: three rounded products summed left to
 // right (no FMA contraction), so boundary pairs classify as in the reference.
@@ -47,22 +57,53 @@ __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
   return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
                    __fmul_rn(dz, dz));
 }
+// Fast estimate of the same value (within a few ulp of dist2).
+__device__ __forceinline__ float dist2_fast(float dx, float dy, float dz) {
+  return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+}
 
 __device__ __forceinline__ void flag(uint32_t* status, uint32_t f) {
   atomicOr(status, f);
 }
 
-// Walk of the 27 neighbour buckets in the reference's order
-// (CalculateDensity :331-363 and the force loops): for each offset cell,
-// scan [start[key], start[key+1]) and keep entries whose float(hash) equals
-// the cell's (the reference stores the hash as a float, :480, :346).
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
+  const uint32_t lane = lane_id();
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, x, d);
+    if (lane >= static_cast<uint32_t>(d)) x += y;
+  }
+  return x;
+}
+
+// Rank among the lanes of the warp that share `key`, and one atomicAdd per
+// distinct key (particles stored in the previous sorted order share cells
+// with their warp neighbours). All 32 lanes must call; inactive lanes pass
+// active = false and get 0.
+__device__ __forceinline__ uint32_t aggregated_rank(uint32_t* count,
+                                                    uint32_t key,
+                                                    bool active) {
+  const uint32_t am = __ballot_sync(kFull, active);
+  if (!active) return 0u;
+  const uint32_t lane = lane_id();
+  const uint32_t peers = __match_any_sync(am, key);
+  const int leader = __ffs(peers) - 1;
+  uint32_t base = 0;
+  if (static_cast<int>(lane) == leader) base = atomicAdd(count + key, __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+// Walk of the 27 neighbour buckets in the reference's order (the loops of
+// CalculateDensity :331-363, CalculatePressureForce :378-419 and
+// CalculateViscosityForce :432-462): scan [start[key], start[key+1]) and keep
+// entries whose float(hash) equals the cell's (the lookup stores the hash as
+// a float, :480, :346). Used where a cell tile does not fit shared memory.
 template <class F>
-__device__ __forceinline__ void walk27(const SceneDev& S,
+__device__ __forceinline__ void walk27(const SceneDev& S, uint32_t hc,
                                        const uint32_t* __restrict__ start,
                                        const float4* __restrict__ pred,
-                                       float3 p, F&& visit) {
-  const uint32_t hc = hash_cell(cell_of(p.x, S.r), cell_of(p.y, S.r),
-                                cell_of(p.z, S.r));
+                                       F&& visit) {
 #pragma unroll 1
   for (int o = 0; o < 27; ++o) {
     const uint32_t h = hc + c_delta[o];
@@ -94,17 +135,21 @@ __global__ void k_predict_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
                                const float4* __restrict__ pos,
                                const float4* __restrict__ vel,
                                uint32_t* __restrict__ count,
-                               uint2* __restrict__ keyrank) {
-  const int lane = threadIdx.x & 31;
+                               uint4* __restrict__ keyrank) {
+  const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev S = scenes[tile_scene(tile)];
+    const SceneDev& S = scenes[tile_scene(tile)];
     const uint32_t s = tile.y + lane;
-    if (static_cast<uint32_t>(lane) >= tile_len(tile)) continue;
-    uint32_t key, hash;
-    predict_key(S, pos[s], vel[s], key, hash);
-    const uint32_t r = atomicAdd(count + key, 1u);
-    keyrank[s] = make_uint2(key, r);
+    const bool live = lane < tile_len(tile);
+    uint32_t key = 0, hash = 0, id = 0;
+    if (live) {
+      const float4 p = pos[s];
+      predict_key(S, p, vel[s], key, hash);
+      id = __float_as_uint(p.w);
+    }
+    const uint32_t r = aggregated_rank(count, key, live);
+    if (live) keyrank[s] = make_uint4(key, r, hash, id);
   }
 }
 
@@ -113,27 +158,17 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanBlock = kScanThreads * kScanItems;
 
-__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-    if (lane >= d) x += y;
-  }
-  return x;
-}
-
 // Block-wide exclusive scan of one value per thread; returns the block total
 // through *total.
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x,
                                                     uint32_t* total) {
   __shared__ uint32_t warp_sums[32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
   const uint32_t incl = warp_incl_scan(x);
   if (lane == 31) warp_sums[w] = incl;
   __syncthreads();
   if (w == 0) {
-    const int nw = blockDim.x >> 5;
+    const uint32_t nw = blockDim.x >> 5;
     uint32_t v = lane < nw ? warp_sums[lane] : 0u;
     v = warp_incl_scan(v);
     warp_sums[lane] = v;
@@ -199,151 +234,284 @@ k_scan_down(uint32_t* __restrict__ count, uint32_t len,
 
 // ----------------------------------------------------------------- scatter
 __global__ void k_scatter(const uint2* __restrict__ tiles, uint32_t ntiles,
-                          const SceneDev* __restrict__ scenes,
-                          const uint2* __restrict__ keyrank,
-                          const uint32_t* __restrict__ start,
-                          const float4* __restrict__ pos, uint32_t total,
-                          uint2* __restrict__ tmp, uint32_t* status) {
-  const int lane = threadIdx.x & 31;
+                          const uint4* __restrict__ keyrank,
+                          const uint32_t* __restrict__ start, uint32_t total,
+                          uint2* __restrict__ tmp_hi,
+                          uint32_t* __restrict__ tmp_src, uint32_t* status) {
+  const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev S = scenes[tile_scene(tile)];
     const uint32_t s = tile.y + lane;
-    if (static_cast<uint32_t>(lane) >= tile_len(tile)) continue;
-    const uint2 kr = keyrank[s];
+    if (lane >= tile_len(tile)) continue;
+    const uint4 kr = keyrank[s];
     const uint32_t dst = start[kr.x] + kr.y;
     if (dst >= total) { flag(status, kStatusRange); continue; }
-    tmp[dst] = make_uint2(__float_as_uint(pos[s].w), s);
+    tmp_hi[dst] = make_uint2(kr.z, kr.w);
+    tmp_src[dst] = s;
   }
 }
 
 // ----------------------------------------------------------------- reorder
-// Thread per bucketed slot t: rank the particle among its bucket by index
-// (canonical (key, index) order), recompute its gravity/prediction exactly
-// as k_predict_hash did, and write the state to its final slot.
+// Thread per bucketed slot: rank the particle inside its bucket by
+// (hash, index), recompute its gravity/prediction exactly as k_predict_hash
+// did, and write the state to its final slot.
 __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
                           const SceneDev* __restrict__ scenes,
-                          const uint2* __restrict__ tmp,
+                          const uint2* __restrict__ tmp_hi,
+                          const uint32_t* __restrict__ tmp_src,
                           const uint32_t* __restrict__ start,
                           const float4* __restrict__ pos_in,
                           const float4* __restrict__ vel_in,
                           float4* __restrict__ pos_out,
                           float4* __restrict__ vel_out,
                           float4* __restrict__ pred,
-                          uint32_t* __restrict__ dbg_hash,
+                          uint32_t* __restrict__ hash_s,
                           uint32_t* __restrict__ dbg_key, uint32_t src_limit,
                           uint32_t* status) {
-  const int lane = threadIdx.x & 31;
+  const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev S = scenes[tile_scene(tile)];
+    const SceneDev& S = scenes[tile_scene(tile)];
     const uint32_t slot = tile.y + lane;
-    if (static_cast<uint32_t>(lane) >= tile_len(tile)) continue;
-    const uint2 me = tmp[slot];
-    if (me.y >= src_limit) { flag(status, kStatusRange); continue; }
-    const float4 p = pos_in[me.y];
-    const float4 v = vel_in[me.y];
+    if (lane >= tile_len(tile)) continue;
+    const uint2 me = tmp_hi[slot];
+    const uint32_t src = tmp_src[slot];
+    if (src >= src_limit) { flag(status, kStatusRange); continue; }
+    const float4 p = pos_in[src];
+    const float4 v = vel_in[src];
     float3 vn, pr;
     predict(S, p, v, vn, pr);
     const uint32_t hash = hash_of(S, pr);
     const uint32_t key = S.base + fastmod(hash, S.fm, S.n);
     const uint32_t b0 = start[key], b1 = start[key + 1];
-    if (slot < b0 || slot >= b1) { flag(status, kStatusRange); continue; }
+    if (slot < b0 || slot >= b1 || hash != me.x) {
+      flag(status, kStatusRange);
+      continue;
+    }
     uint32_t rank = 0;
-    for (uint32_t u = b0; u < b1; ++u) rank += (tmp[u].x < me.x) ? 1u : 0u;
+    for (uint32_t u = b0; u < b1; ++u) {
+      const uint2 o = tmp_hi[u];
+      rank += (o.x < me.x || (o.x == me.x && o.y < me.y)) ? 1u : 0u;
+    }
     const uint32_t f = b0 + rank;
     pos_out[f] = p;
     vel_out[f] = make_float4(vn.x, vn.y, vn.z, 0.0f);
     pred[f] = make_float4(pr.x, pr.y, pr.z, __uint2float_rn(hash));
-    if (dbg_hash) {
-      dbg_hash[f] = hash;
-      dbg_key[f] = key - S.base;
-    }
+    hash_s[f] = hash;
+    if (dbg_key) dbg_key[f] = key - S.base;
   }
 }
 
 // ----------------------------------------------------------------- density
-// CalculateDensity (:325-365), self included. The kernel condition
-// `sqrDist <= sqrRadius && dist < r` is the exact float test d2 <= cut_lt.
-__global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
-                          const SceneDev* __restrict__ scenes,
-                          const float4* __restrict__ pred,
-                          const uint32_t* __restrict__ start,
-                          float2* __restrict__ dens_a,
-                          float4* __restrict__ dens_b) {
-  const int lane = threadIdx.x & 31;
+// Per-pair test shared by the density pass: exact classification of the
+// reference's conditions `sqrDist <= sqrRadius` and `dist < r` / `dist <= r`
+// (kernels.h:27,51) on the non-contracted squared distance.
+struct NbrSink {
+  uint32_t* nbr;
+  uint32_t stride;
+  uint32_t cap;
+};
+
+// CalculateDensity (:325-365) for one particle over a candidate stream, and
+// the particle's neighbour list (pairs with dist <= r, self excluded) for
+// the force passes.
+struct DensityAcc {
+  float s2 = 0.0f, s3 = 0.0f;
+  uint32_t cnt = 0;
+  __device__ __forceinline__ void visit(const SceneDev& S, float3 p,
+                                        uint32_t i, uint32_t j, float4 q,
+                                        const NbrSink& L) {
+    const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+    const float d2f = dist2_fast(dx, dy, dz);
+    if (d2f <= S.cut_hi) {
+      const float d2 = dist2(dx, dy, dz);
+      if (d2 <= S.cut_le) {
+        if (j != i) {
+          if (cnt < L.cap) L.nbr[cnt * L.stride + i] = j;
+          ++cnt;
+        }
+        if (d2 <= S.cut_lt) {
+          const float w = S.r - __fsqrt_rn(d2);
+          const float w2 = w * w;
+          s2 += w2;
+          s3 = fmaf(w2, w, s3);
+        }
+      }
+    }
+  }
+};
+
+__device__ __forceinline__ void density_finish(const SceneDev& S, uint32_t i,
+                                               const DensityAcc& a,
+                                               float2* __restrict__ dens_a,
+                                               float4* __restrict__ dens_b,
+                                               uint32_t* __restrict__ ncount) {
+  const float rho = a.s2 * S.vol2, rhon = a.s3 * S.vol3;
+  dens_a[i] = make_float2(rho, rhon);
+  const float ir = 1.0f / rho, irn = 1.0f / rhon;
+  const float P = (rho - S.rho0) * S.k, Pn = rhon * S.kn;
+  dens_b[i] = make_float4(ir, P * ir, irn, Pn * irn);
+  ncount[i] = a.cnt;
+}
+
+// Cell tiles: each warp takes 32 consecutive slots, finds the cells (runs of
+// equal hash) among them and stages every cell's 27 neighbour buckets once
+// into its shared-memory tile (entries of a different float(hash) become
+// +inf so they fail the distance test; .w carries the slot). Each lane then
+// tests its particle against its cell's staged candidates. Cells whose
+// candidates do not fit the tile walk global memory instead.
+template <int kWarps>
+__global__ void __launch_bounds__(kWarps * 32)
+k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
+          const SceneDev* __restrict__ scenes, const float4* __restrict__ pred,
+          const uint32_t* __restrict__ hash_s,
+          const uint32_t* __restrict__ start, float2* __restrict__ dens_a,
+          float4* __restrict__ dens_b, uint32_t* __restrict__ nbr,
+          uint32_t* __restrict__ ncount, uint32_t nbr_stride, uint32_t nbr_cap,
+          uint32_t tile_cap) {
+  extern __shared__ float4 s_cand_all[];
+  __shared__ uint32_t s_off[kWarps][33];
+  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+  float4* cand = s_cand_all + w * tile_cap;
+  const NbrSink L{nbr, nbr_stride, nbr_cap};
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev S = scenes[tile_scene(tile)];
+    const SceneDev& S = scenes[tile_scene(tile)];
+    const bool live = lane < tile_len(tile);
     const uint32_t i = tile.y + lane;
-    if (static_cast<uint32_t>(lane) >= tile_len(tile)) continue;
-    const float4 pi = pred[i];
-    const float3 p = make_float3(pi.x, pi.y, pi.z);
-    float s2 = 0.0f, s3 = 0.0f;
-    walk27(S, start, pred, p, [&](uint32_t, float4 q) {
-      const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-      const float d2 = dist2(dx, dy, dz);
-      if (d2 <= S.cut_lt) {
-        const float w = S.r - __fsqrt_rn(d2);
-        const float w2 = w * w;
-        s2 += w2;
-        s3 += w2 * w;
+    const float4 me = live ? pred[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t h = live ? hash_s[i] : 0u;
+    const uint32_t hprev = __shfl_up_sync(kFull, h, 1);
+    const bool leader = live && (lane == 0 || h != hprev);
+    const uint32_t lmask = __ballot_sync(kFull, leader);
+    const int ncell = __popc(lmask);
+    const int mycell = __popc(lmask & ((2u << lane) - 1u)) - 1;
+    const float3 p = make_float3(me.x, me.y, me.z);
+    DensityAcc acc;
+    int c0 = 0;
+    while (c0 < ncell) {
+      // stage cells c0.. while they fit the tile
+      uint32_t used = 0, ovf = 0;
+      int c1 = c0;
+      for (; c1 < ncell; ++c1) {
+        const int Ld = __fns(lmask, 0, c1 + 1);
+        const uint32_t hc = __shfl_sync(kFull, h, Ld);
+        uint32_t b0 = 0, cnt = 0;
+        float hf = 0.0f;
+        if (lane < 27) {
+          const uint32_t hh = hc + c_delta[lane];
+          const uint32_t key = S.base + fastmod(hh, S.fm, S.n);
+          b0 = __ldg(start + key);
+          cnt = __ldg(start + key + 1) - b0;
+          hf = __uint2float_rn(hh);
+        }
+        const uint32_t incl = warp_incl_scan(cnt);
+        const uint32_t m = __shfl_sync(kFull, incl, 31);
+        if (lane == 0) s_off[w][c1 - c0] = used;
+        if (m > tile_cap) {  // this cell alone exceeds the tile
+          ovf |= 1u << (c1 - c0);
+          continue;
+        }
+        if (used + m > tile_cap) break;  // next round
+        float4* dst = cand + used + (incl - cnt);
+        for (uint32_t k = 0; k < cnt; ++k) {
+          float4 q = __ldg(pred + b0 + k);
+          if (q.w != hf) q.x = kInf;
+          q.w = __uint_as_float(b0 + k);
+          dst[k] = q;
+        }
+        used += m;
       }
-    });
-    const float rho = s2 * S.vol2, rhon = s3 * S.vol3;
-    dens_a[i] = make_float2(rho, rhon);
-    const float ir = 1.0f / rho, irn = 1.0f / rhon;
-    const float P = (rho - S.rho0) * S.k, Pn = rhon * S.kn;
-    dens_b[i] = make_float4(ir, P * ir, irn, Pn * irn);
+      if (lane == 0) s_off[w][c1 - c0] = used;
+      __syncwarp();
+      if (live && mycell >= c0 && mycell < c1) {
+        const int lc = mycell - c0;
+        if ((ovf >> lc) & 1u) {
+          walk27(S, h, start, pred, [&](uint32_t j, float4 q) {
+            acc.visit(S, p, i, j, q, L);
+          });
+        } else {
+          const uint32_t k0 = s_off[w][lc], k1 = s_off[w][lc + 1];
+#pragma unroll 4
+          for (uint32_t k = k0; k < k1; ++k) {
+            const float4 q = cand[k];
+            acc.visit(S, p, i, __float_as_uint(q.w), q, L);
+          }
+        }
+      }
+      __syncwarp();
+      c0 = c1;
+    }
+    if (live) density_finish(S, i, acc, dens_a, dens_b, ncount);
   }
 }
 
 // ---------------------------------------------------------------- pressure
-// CalculatePressureForce (:367-422), self skipped. The shared pressure over
-// the neighbour's density is 0.5*(Pi + Pj)/rho_j = 0.5*(Pi*(1/rho_j) +
-// Pj/rho_j); the 0.5 is folded into ds2h/ds3h.
+// CalculatePressureForce (:367-422) over the particle's neighbour list (self
+// excluded, dist <= r). shared/rho_j = 0.5*(Pi*(1/rho_j) + Pj/rho_j); the 0.5
+// is folded into ds2h/ds3h. A list that overflowed falls back to the walk.
+__device__ __forceinline__ void pressure_pair(const SceneDev& S, float3 p,
+                                              float Pi, float Pni, float4 q,
+                                              float4 b, float3& f) {
+  const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+  const float d2 = dist2(dx, dy, dz);
+  const float dist = __fsqrt_rn(d2);
+  const float w = S.r - dist;
+  const float a2 = S.ds2h * fmaf(Pi, b.x, b.y);
+  const float a3 = S.ds3h * w * fmaf(Pni, b.z, b.w);
+  const float tsum = -w * (a2 + a3);
+  if (d2 > 0.0f) {
+    const float s = tsum * rsqrtf(d2);
+    f.x = fmaf(dx, s, f.x);
+    f.y = fmaf(dy, s, f.y);
+    f.z = fmaf(dz, s, f.z);
+  } else {
+    f.y += tsum;  // dir = (0,1,0) for coincident particles (:414)
+  }
+}
+
 __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
                            const SceneDev* __restrict__ scenes,
                            const float4* __restrict__ pred,
+                           const uint32_t* __restrict__ hash_s,
                            const uint32_t* __restrict__ start,
                            const float2* __restrict__ dens_a,
                            const float4* __restrict__ dens_b,
+                           const uint32_t* __restrict__ nbr,
+                           const uint32_t* __restrict__ ncount,
+                           uint32_t nbr_stride, uint32_t nbr_cap,
                            const float4* __restrict__ vel,
                            float4* __restrict__ velp,
                            float4* __restrict__ dbg_accp) {
-  const int lane = threadIdx.x & 31;
+  const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev S = scenes[tile_scene(tile)];
+    const SceneDev& S = scenes[tile_scene(tile)];
     const uint32_t i = tile.y + lane;
-    if (static_cast<uint32_t>(lane) >= tile_len(tile)) continue;
+    if (lane >= tile_len(tile)) continue;
     const float4 pi = pred[i];
     const float3 p = make_float3(pi.x, pi.y, pi.z);
     const float2 di = dens_a[i];
     const float Pi = (di.x - S.rho0) * S.k, Pni = di.y * S.kn;
-    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    walk27(S, start, pred, p, [&](uint32_t j, float4 q) {
-      if (j == i) return;
-      const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-      const float d2 = dist2(dx, dy, dz);
-      if (d2 <= S.cut_le) {
-        const float4 b = __ldg(dens_b + j);
-        const float dist = __fsqrt_rn(d2);
-        const float inv = d2 > 0.0f ? rsqrtf(d2) : 0.0f;
-        const float w = S.r - dist;
-        const float a2 = S.ds2h * fmaf(Pi, b.x, b.y);
-        const float a3 = S.ds3h * w * fmaf(Pni, b.z, b.w);
-        const float tsum = -w * (a2 + a3);
-        if (d2 > 0.0f) {
-          const float s = tsum * inv;
-          fx += dx * s; fy += dy * s; fz += dz * s;
-        } else {
-          fy += tsum;  // dir = (0,1,0) for coincident particles (:414)
-        }
+    float3 f = make_float3(0.0f, 0.0f, 0.0f);
+    const uint32_t cnt = ncount[i];
+    if (cnt <= nbr_cap) {
+      const uint32_t* row = nbr + i;
+#pragma unroll 2
+      for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t j = __ldg(row + k * nbr_stride);
+        pressure_pair(S, p, Pi, Pni, __ldg(pred + j), __ldg(dens_b + j), f);
       }
-    });
+    } else {
+      walk27(S, hash_s[i], start, pred, [&](uint32_t j, float4 q) {
+        if (j == i) return;
+        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+        if (dist2(dx, dy, dz) <= S.cut_le)
+          pressure_pair(S, p, Pi, Pni, q, __ldg(dens_b + j), f);
+      });
+    }
     const float inv_rho = 1.0f / di.x;
-    const float ax = fx * inv_rho, ay = fy * inv_rho, az = fz * inv_rho;
+    const float ax = f.x * inv_rho, ay = f.y * inv_rho, az = f.z * inv_rho;
     const float4 v = vel[i];
     velp[i] = make_float4(v.x + ax * S.dt, v.y + ay * S.dt, v.z + az * S.dt, 0.f);
     if (dbg_accp) dbg_accp[i] = make_float4(ax, ay, az, 0.0f);
@@ -351,46 +519,63 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
 }
 
 // ------------------------------------------------ viscosity + integrate
-// CalculateViscosityForce (:424-464) reading the post-pressure snapshot
-// (Jacobi), then pos += v*dt and the box collision (:81-108). poly6 uses
-// r^2 - d2 for r*r - dist*dist. With next_dt > 0 the next substep's
-// prediction/hash/histogram (k_predict_hash) runs here on the new state.
+// CalculateViscosityForce (:424-464) over the neighbour list reading the
+// post-pressure snapshot (Jacobi); poly6 = (r^2 - d^2)^3 for dist < r. Then
+// pos += v*dt and the box collision (:81-108). With fuse_next the next
+// substep's prediction / hash / histogram (k_predict_hash) runs here on the
+// new state.
+__device__ __forceinline__ void visc_pair(const SceneDev& S, float3 p,
+                                          float4 vi, float4 q, float4 vj,
+                                          float3& f) {
+  const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+  const float d2 = dist2(dx, dy, dz);
+  if (d2 <= S.cut_lt) {
+    const float w = S.r2 - d2;
+    const float w3 = w * w * w;
+    f.x = fmaf(vj.x - vi.x, w3, f.x);
+    f.y = fmaf(vj.y - vi.y, w3, f.y);
+    f.z = fmaf(vj.z - vi.z, w3, f.z);
+  }
+}
+
 __global__ void k_visc_integrate(
     const uint2* __restrict__ tiles, uint32_t ntiles,
     const SceneDev* __restrict__ scenes, const float4* __restrict__ pred,
-    const uint32_t* __restrict__ start, const float4* __restrict__ velp,
+    const uint32_t* __restrict__ hash_s, const uint32_t* __restrict__ start,
+    const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ ncount,
+    uint32_t nbr_stride, uint32_t nbr_cap, const float4* __restrict__ velp,
     float4* __restrict__ pos, float4* __restrict__ vel,
     float4* __restrict__ out4, int fuse_next, uint32_t* __restrict__ count,
-    uint2* __restrict__ keyrank, float4* __restrict__ dbg_velv,
+    uint4* __restrict__ keyrank, float4* __restrict__ dbg_velv,
     uint32_t* status) {
-  const int lane = threadIdx.x & 31;
+  const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev S = scenes[tile_scene(tile)];
+    const SceneDev& S = scenes[tile_scene(tile)];
     const uint32_t i = tile.y + lane;
-    const bool live = static_cast<uint32_t>(lane) < tile_len(tile);
+    const bool live = lane < tile_len(tile);
     bool bad = false;
+    uint32_t key = 0, hash = 0, id = 0;
     if (live) {
       const float4 pi = pred[i];
       const float3 p = make_float3(pi.x, pi.y, pi.z);
       const float4 vi = velp[i];
-      float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-      walk27(S, start, pred, p, [&](uint32_t j, float4 q) {
-        if (j == i) return;
-        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-        const float d2 = dist2(dx, dy, dz);
-        if (d2 <= S.cut_lt) {
-          const float dist = __fsqrt_rn(d2);
-          const float w = __fsub_rn(S.r2, __fmul_rn(dist, dist));
-          const float w3 = w * w * w;
-          const float4 vj = __ldg(velp + j);
-          fx += (vj.x - vi.x) * w3;
-          fy += (vj.y - vi.y) * w3;
-          fz += (vj.z - vi.z) * w3;
+      float3 f = make_float3(0.0f, 0.0f, 0.0f);
+      const uint32_t cnt = ncount[i];
+      if (cnt <= nbr_cap) {
+        const uint32_t* row = nbr + i;
+#pragma unroll 2
+        for (uint32_t k = 0; k < cnt; ++k) {
+          const uint32_t j = __ldg(row + k * nbr_stride);
+          visc_pair(S, p, vi, __ldg(pred + j), __ldg(velp + j), f);
         }
-      });
+      } else {
+        walk27(S, hash_s[i], start, pred, [&](uint32_t j, float4 q) {
+          if (j != i) visc_pair(S, p, vi, q, __ldg(velp + j), f);
+        });
+      }
       const float c = S.vscale * S.mu * S.dt;
-      float3 v = make_float3(vi.x + fx * c, vi.y + fy * c, vi.z + fz * c);
+      float3 v = make_float3(vi.x + f.x * c, vi.y + f.y * c, vi.z + f.z * c);
       if (dbg_velv) dbg_velv[i] = make_float4(v.x, v.y, v.z, 0.0f);
       float4 x = pos[i];
       x.x = __fadd_rn(x.x, __fmul_rn(v.x, S.dt));
@@ -405,19 +590,18 @@ __global__ void k_visc_integrate(
       vel[i] = v4;
       bad = !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) &&
               isfinite(v.x) && isfinite(v.y) && isfinite(v.z));
+      id = __float_as_uint(x.w);
       if (out4) {
-        const uint32_t id = __float_as_uint(x.w);
         if (id < S.n) out4[S.base + id] = make_float4(x.x, x.y, x.z, 0.34f);
         else bad = true;
       }
-      if (fuse_next) {
-        uint32_t key, hash;
-        predict_key(S, x, v4, key, hash);
-        const uint32_t r = atomicAdd(count + key, 1u);
-        keyrank[i] = make_uint2(key, r);
-      }
+      if (fuse_next) predict_key(S, x, v4, key, hash);
     }
-    if (__any_sync(0xffffffffu, bad) && lane == 0) flag(status, kStatusNonFinite);
+    if (fuse_next) {
+      const uint32_t r = aggregated_rank(count, key, live);
+      if (live) keyrank[i] = make_uint4(key, r, hash, id);
+    }
+    if (__any_sync(kFull, bad) && lane == 0) flag(status, kStatusNonFinite);
   }
 }
 
@@ -435,8 +619,8 @@ __global__ void k_export(uint32_t first, uint32_t n,
   const uint32_t s = first + k;
   const float4 p = pos[s];
   const uint32_t id = __float_as_uint(p.w);
-  if (id >= n) return;
   if (oids) oids[k] = id;
+  if (id >= n) return;
   if (opos) { opos[3 * id] = p.x; opos[3 * id + 1] = p.y; opos[3 * id + 2] = p.z; }
   if (ovel) {
     const float4 v = vel[s];
@@ -495,8 +679,9 @@ __global__ void k_import(uint32_t first, uint32_t n,
 cudaError_t launch_predict_hash(const LaunchCtx& c, const Tiles& old_tiles,
                                 cudaStream_t st) {
   if (old_tiles.n == 0) return cudaSuccess;
-  k_predict_hash<<<grid_for(old_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
-      old_tiles.d, old_tiles.n, c.scenes, c.pos, c.vel, c.count, c.keyrank);
+  k_predict_hash<<<grid_for(old_tiles.n, c.block_misc, c.max_blocks),
+                   c.block_misc, 0, st>>>(old_tiles.d, old_tiles.n, c.scenes,
+                                          c.pos, c.vel, c.count, c.keyrank);
   return cudaGetLastError();
 }
 
@@ -518,23 +703,39 @@ cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
                                 cudaStream_t st) {
   if (old_tiles.n) {
     k_scatter<<<grid_for(old_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
-        old_tiles.d, old_tiles.n, c.scenes, c.keyrank, c.start, c.pos, total,
-        c.tmp, c.status);
+        old_tiles.d, old_tiles.n, c.keyrank, c.start, total, c.tmp_hi,
+        c.tmp_src, c.status);
   }
   if (new_tiles.n) {
     k_reorder<<<grid_for(new_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
-        new_tiles.d, new_tiles.n, c.scenes, c.tmp, c.start, c.pos, c.vel,
-        c.pos2, c.vel2, c.pred, c.dbg_hash, c.dbg_key, c.src_limit, c.status);
+        new_tiles.d, new_tiles.n, c.scenes, c.tmp_hi, c.tmp_src, c.start, c.pos,
+        c.vel, c.pos2, c.vel2, c.pred, c.hash_s, c.dbg_key, c.src_limit,
+        c.status);
   }
   return cudaGetLastError();
+}
+
+constexpr int kDensityWarps = 4;
+
+size_t density_smem_bytes(int tile_cap) {
+  return static_cast<size_t>(kDensityWarps) * tile_cap * sizeof(float4);
+}
+
+cudaError_t density_configure(int tile_cap) {
+  return cudaFuncSetAttribute(k_density<kDensityWarps>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(density_smem_bytes(tile_cap)));
 }
 
 cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
                            cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
-  const int b = c.block_nbr;
-  k_density<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.start, c.dens_a, c.dens_b);
+  const int b = kDensityWarps * 32;
+  k_density<kDensityWarps><<<grid_for(tiles.n, b, c.max_blocks), b,
+                             density_smem_bytes(c.tile_cap), st>>>(
+      tiles.d, tiles.n, c.scenes, c.pred, c.hash_s, c.start, c.dens_a,
+      c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap,
+      static_cast<uint32_t>(c.tile_cap));
   return cudaGetLastError();
 }
 
@@ -543,8 +744,9 @@ cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_nbr;
   k_pressure<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.start, c.dens_a, c.dens_b, c.vel2,
-      c.velp, c.dbg_accp);
+      tiles.d, tiles.n, c.scenes, c.pred, c.hash_s, c.start, c.dens_a,
+      c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap, c.vel2, c.velp,
+      c.dbg_accp);
   return cudaGetLastError();
 }
 
@@ -554,7 +756,8 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_nbr;
   k_visc_integrate<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.start, c.velp, c.pos2, c.vel2,
+      tiles.d, tiles.n, c.scenes, c.pred, c.hash_s, c.start, c.nbr, c.ncount,
+      c.nbr_stride, c.nbr_cap, c.velp, c.pos2, c.vel2,
       write_out ? c.out4 : nullptr, fuse_next, c.count, c.keyrank, c.dbg_velv,
       c.status);
   return cudaGetLastError();

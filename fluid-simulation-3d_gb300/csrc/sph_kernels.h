@@ -47,20 +47,26 @@ struct LaunchCtx {
   float4* velp = nullptr;
   float2* dens_a = nullptr;
   float4* dens_b = nullptr;
-  uint2* keyrank = nullptr;
-  uint2* tmp = nullptr;
+  uint4* keyrank = nullptr;   // (key, arrival rank, hash, id) per old slot
+  uint2* tmp_hi = nullptr;    // (hash, id) per bucketed slot
+  uint32_t* tmp_src = nullptr;  // source slot per bucketed slot
+  uint32_t* hash_s = nullptr;   // cell hash per sorted slot
   uint32_t* count = nullptr;
   uint32_t* start = nullptr;
   uint32_t* partial = nullptr;
+  uint32_t* nbr = nullptr;      // neighbour lists, nbr[k * nbr_stride + slot]
+  uint32_t* ncount = nullptr;   // neighbours per slot (> nbr_cap: overflow)
+  uint32_t nbr_stride = 0;
+  uint32_t nbr_cap = 0;
+  int tile_cap = 1024;          // candidates per warp's shared-memory tile
   float4* out4 = nullptr;
   uint32_t* status = nullptr;
-  uint32_t* dbg_hash = nullptr;
   uint32_t* dbg_key = nullptr;
   float4* dbg_accp = nullptr;
   float4* dbg_velv = nullptr;
   uint32_t src_limit = 0;  // slots of the layout a substep reads
   int block_misc = 256;   // predict/scatter/reorder
-  int block_nbr = 128;    // neighbour kernels
+  int block_nbr = 128;    // list-based force kernels
   uint32_t max_blocks = 0;  // persistent grid cap (0 = no cap)
 };
 
@@ -79,6 +85,10 @@ cudaError_t launch_scan(const LaunchCtx& c, uint32_t len, cudaStream_t st);
 cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
                                 const Tiles& new_tiles, uint32_t total,
                                 cudaStream_t st);
+// Dynamic shared memory of the density kernel for a given tile capacity;
+// density_configure raises the kernel's shared-memory limit accordingly.
+size_t density_smem_bytes(int tile_cap);
+cudaError_t density_configure(int tile_cap);
 cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
                            cudaStream_t st);
 cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
