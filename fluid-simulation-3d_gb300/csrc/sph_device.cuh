@@ -36,6 +36,8 @@ struct SceneDev {
   float cut_le;       // d2 <= cut_le  <=>  d2 <= sqrRadius && sqrtf(d2) <= r
   float cut_hi;       // cut_le widened by 2e-6 relative: bounds the FMA
                       // estimate of d2 for every pair with d2 <= cut_le
+  float cut_lo;       // cut_lt narrowed by 2e-6: an FMA estimate below it
+                      // certifies d2 <= cut_lt without the exact recompute
   float r2;           // r*r
   float vol2, vol3;   // density kernel scales   (kernels.h:28,40)
   float ds2h, ds3h;   // 0.5 * derivative scales (kernels.h:52,64)

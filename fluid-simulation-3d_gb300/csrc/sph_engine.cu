@@ -39,6 +39,7 @@ SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base,
   d.cut_lt = std::min(p.cutoff_sq, t_lt);
   d.cut_le = std::min(p.cutoff_sq, t_le);
   d.cut_hi = d.cut_le * 1.000002f;
+  d.cut_lo = d.cut_lt * 0.999998f;
   d.r2 = r * r;
   // kernels.h:28,40,52,64,76 -- same float expressions.
   d.vol2 = 15.0f / (2.0f * kPiF * powf(r, 5.0f));
@@ -83,7 +84,8 @@ Engine::~Engine() {
   void* ptrs[] = {d_scenes_, d_tiles_old_, d_tiles_new_, d_pos_[0], d_pos_[1],
                   d_vel_[0], d_vel_[1], ctx_.pred, ctx_.velp, ctx_.dens_a,
                   ctx_.dens_b, ctx_.keyrank, ctx_.tmp_hi, ctx_.tmp_src, ctx_.hash_s,
-                  ctx_.nbr, ctx_.ncount, ctx_.count, ctx_.start,
+                  ctx_.nbr, ctx_.ncount, ctx_.cell_first, ctx_.cell_tab,
+                  ctx_.count, ctx_.start,
                   ctx_.partial, d_out4_, d_status_, d_dbg_hash_, d_dbg_key_,
                   d_dbg_accp_, d_dbg_velv_, d_dbg_velp_, d_dbg_start_,
                   d_dbg_scratch_};
@@ -141,6 +143,8 @@ int Engine::Init() {
   chk(Alloc(&ctx_.tmp_src, C));
   chk(Alloc(&ctx_.hash_s, C));
   chk(Alloc(&ctx_.ncount, C));
+  chk(Alloc(&ctx_.cell_first, C));
+  chk(Alloc(&ctx_.cell_tab, C * 27ull));
   chk(Alloc(&ctx_.nbr, C * static_cast<uint64_t>(kNbrCap)));
   chk(Alloc(&ctx_.count, C));
   chk(Alloc(&ctx_.start, C + 1));
@@ -162,7 +166,6 @@ int Engine::Init() {
   ctx_.status = d_status_;
   ctx_.nbr_stride = static_cast<uint32_t>(C);
   ctx_.nbr_cap = kNbrCap;
-  SPH_CUDA(density_configure(tuning_.cell_tile), "cudaFuncSetAttribute");
   return SPH_OK;
 }
 
@@ -342,7 +345,7 @@ int Engine::UploadScenes(int substeps, cudaStream_t st) {
 int Engine::RunSubsteps(int substeps, cudaStream_t st) {
   LaunchCtx c = ctx_;
   c.block_nbr = tuning_.block;
-  c.tile_cap = tuning_.cell_tile;
+  c.gather = tuning_.cell_tile;
   c.max_blocks = 0;
   c.src_limit = static_cast<uint32_t>(capacity_);
   int cur = cur_;
@@ -639,14 +642,11 @@ int Engine::SetTuning(const sph_tuning& t) {
     return Fail(SPH_ERR_INVALID, "block must be a multiple of 32 in [32, 1024]");
   if (t.particles_per_warp != 32)
     return Fail(SPH_ERR_INVALID, "particles_per_warp must be 32");
-  // 4 warps per density block share the SM's 227 KB of shared memory
-  if (t.cell_tile < 128 || t.cell_tile > 3456 || (t.cell_tile & 31))
-    return Fail(SPH_ERR_INVALID, "cell_tile must be a multiple of 32 in [128, 3456]");
+  if (t.cell_tile != 2 && t.cell_tile != 4 && t.cell_tile != 8)
+    return Fail(SPH_ERR_INVALID, "cell_tile must be 2, 4 or 8");
   if (t.block != tuning_.block || t.particles_per_warp != tuning_.particles_per_warp ||
       t.cell_tile != tuning_.cell_tile)
     ReleaseGraphs();
-  if (t.cell_tile != tuning_.cell_tile)
-    SPH_CUDA(density_configure(t.cell_tile), "cudaFuncSetAttribute");
   tuning_ = t;
   return SPH_OK;
 }
@@ -656,7 +656,7 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
   if (steps_per_trial < 1) return Fail(SPH_ERR_INVALID, "steps_per_trial >= 1");
   std::vector<sph_tuning> space;
   for (int b : {64, 128, 256, 512})
-    for (int tile : {512, 1024, 2048}) space.push_back(sph_tuning{b, tile, 32});
+    for (int tile : {2, 4, 8}) space.push_back(sph_tuning{b, tile, 32});
   sph_tuning win = tuning_;
   float win_ms = std::numeric_limits<float>::infinity();
   cudaEvent_t e0, e1;

@@ -7,17 +7,18 @@
 //   k_scatter        bucket each particle at start[key] + arrival rank
 //   k_reorder        deterministic order inside each bucket and gather of
 //                    the state into SoA float4                :484-496
-//   k_density        cell tiles staged in shared memory; density / near
-//                    density and each particle's neighbour list :304-365
+//   k_cell_table     per cell, its 27 neighbour runs (the bucket walk of
+//                    :331-346 resolved once per cell instead of per particle)
+//   k_density        density / near density and neighbour lists :304-365
 //   k_pressure       pressure + near pressure over the list   :367-422
 //   k_visc_integrate Jacobi viscosity over the list, integrate, box
 //                    collision, next substep's prediction    :424-464, :81-108
 //
-// Inside a key bucket particles are ordered by (cell hash, index): each cell
-// is a contiguous run (the reference orders a bucket only by key; its
-// canonical (key, index) order is rebuilt from this one on export). Every
-// kernel is a persistent, segmented launch: warps stride over a tile table
-// of (scene, first slot) runs of up to 32 particles of one scene, so one
+// Inside a key bucket particles are ordered by (cell hash, index), so every
+// cell is a contiguous run of slots (the reference orders a bucket only by
+// key; its canonical (key, index) order is rebuilt from this one on export).
+// Every kernel is a persistent, segmented launch: warps stride over a tile
+// table of (scene, first slot) runs of up to 32 particles of one scene, so one
 // launch serves any number of scenes of uneven sizes.
 #include "sph_kernels.h"
 
@@ -26,7 +27,6 @@ namespace sph {
 namespace {
 
 constexpr uint32_t kFull = 0xffffffffu;
-constexpr float kInf = __builtin_huge_valf();
 
 constexpr uint32_t Delta(int o) {
   return static_cast<uint32_t>(o / 9 - 1) * kHashX +
@@ -61,6 +61,12 @@ __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
 __device__ __forceinline__ float dist2_fast(float dx, float dy, float dz) {
   return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
 }
+// Hardware square root estimate (sqrt.approx.f32: 0 -> 0).
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
 __device__ __forceinline__ void flag(uint32_t* status, uint32_t f) {
   atomicOr(status, f);
@@ -94,29 +100,20 @@ __device__ __forceinline__ uint32_t aggregated_rank(uint32_t* count,
   return base + __popc(peers & ((1u << lane) - 1u));
 }
 
-// Walk of the 27 neighbour buckets in the reference's order (the loops of
-// CalculateDensity :331-363, CalculatePressureForce :378-419 and
-// CalculateViscosityForce :432-462): scan [start[key], start[key+1]) and keep
-// entries whose float(hash) equals the cell's (the lookup stores the hash as
-// a float, :480, :346). Used where a cell tile does not fit shared memory.
+// Neighbour walk of a particle through its cell's 27 runs (table built by
+// k_cell_table): every candidate the reference's bucket loops would accept,
+// in the reference's offset order.
 template <class F>
-__device__ __forceinline__ void walk27(const SceneDev& S, uint32_t hc,
-                                       const uint32_t* __restrict__ start,
-                                       const float4* __restrict__ pred,
-                                       F&& visit) {
+__device__ __forceinline__ void walk_runs(const uint2* __restrict__ cell_tab,
+                                          uint32_t cf,
+                                          const float4* __restrict__ pred,
+                                          F&& visit) {
+  const uint2* row = cell_tab + static_cast<uint64_t>(cf) * 27u;
 #pragma unroll 1
   for (int o = 0; o < 27; ++o) {
-    const uint32_t h = hc + c_delta[o];
-    const uint32_t key = S.base + fastmod(h, S.fm, S.n);
-    const float hf = __uint2float_rn(h);
-    const uint32_t b0 = __ldg(start + key);
-    const uint32_t b1 = __ldg(start + key + 1);
+    const uint2 run = __ldg(row + o);
 #pragma unroll 1
-    for (uint32_t j = b0; j < b1; ++j) {
-      const float4 q = __ldg(pred + j);
-      if (q.w != hf) continue;
-      visit(j, q);
-    }
+    for (uint32_t j = run.x; j < run.x + run.y; ++j) visit(j, __ldg(pred + j));
   }
 }
 
@@ -254,7 +251,8 @@ __global__ void k_scatter(const uint2* __restrict__ tiles, uint32_t ntiles,
 // ----------------------------------------------------------------- reorder
 // Thread per bucketed slot: rank the particle inside its bucket by
 // (hash, index), recompute its gravity/prediction exactly as k_predict_hash
-// did, and write the state to its final slot.
+// did, and write the state to its final slot, plus the first slot of its
+// cell (its run of equal hash).
 __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
                           const SceneDev* __restrict__ scenes,
                           const uint2* __restrict__ tmp_hi,
@@ -266,6 +264,7 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
                           float4* __restrict__ vel_out,
                           float4* __restrict__ pred,
                           uint32_t* __restrict__ hash_s,
+                          uint32_t* __restrict__ cell_first,
                           uint32_t* __restrict__ dbg_key, uint32_t src_limit,
                           uint32_t* status) {
   const uint32_t lane = lane_id();
@@ -288,9 +287,10 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
       flag(status, kStatusRange);
       continue;
     }
-    uint32_t rank = 0;
+    uint32_t rank = 0, below = 0;
     for (uint32_t u = b0; u < b1; ++u) {
       const uint2 o = tmp_hi[u];
+      below += (o.x < me.x) ? 1u : 0u;
       rank += (o.x < me.x || (o.x == me.x && o.y < me.y)) ? 1u : 0u;
     }
     const uint32_t f = b0 + rank;
@@ -298,158 +298,147 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
     vel_out[f] = make_float4(vn.x, vn.y, vn.z, 0.0f);
     pred[f] = make_float4(pr.x, pr.y, pr.z, __uint2float_rn(hash));
     hash_s[f] = hash;
+    cell_first[f] = b0 + below;
     if (dbg_key) dbg_key[f] = key - S.base;
   }
 }
 
-// ----------------------------------------------------------------- density
-// Per-pair test shared by the density pass: exact classification of the
-// reference's conditions `sqrDist <= sqrRadius` and `dist < r` / `dist <= r`
-// (kernels.h:27,51) on the non-contracted squared distance.
-struct NbrSink {
-  uint32_t* nbr;
-  uint32_t stride;
-  uint32_t cap;
-};
-
-// CalculateDensity (:325-365) for one particle over a candidate stream, and
-// the particle's neighbour list (pairs with dist <= r, self excluded) for
-// the force passes.
-struct DensityAcc {
-  float s2 = 0.0f, s3 = 0.0f;
-  uint32_t cnt = 0;
-  __device__ __forceinline__ void visit(const SceneDev& S, float3 p,
-                                        uint32_t i, uint32_t j, float4 q,
-                                        const NbrSink& L) {
-    const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-    const float d2f = dist2_fast(dx, dy, dz);
-    if (d2f <= S.cut_hi) {
-      const float d2 = dist2(dx, dy, dz);
-      if (d2 <= S.cut_le) {
-        if (j != i) {
-          if (cnt < L.cap) L.nbr[cnt * L.stride + i] = j;
-          ++cnt;
-        }
-        if (d2 <= S.cut_lt) {
-          const float w = S.r - __fsqrt_rn(d2);
-          const float w2 = w * w;
-          s2 += w2;
-          s3 = fmaf(w2, w, s3);
-        }
-      }
-    }
-  }
-};
-
-__device__ __forceinline__ void density_finish(const SceneDev& S, uint32_t i,
-                                               const DensityAcc& a,
-                                               float2* __restrict__ dens_a,
-                                               float4* __restrict__ dens_b,
-                                               uint32_t* __restrict__ ncount) {
-  const float rho = a.s2 * S.vol2, rhon = a.s3 * S.vol3;
-  dens_a[i] = make_float2(rho, rhon);
-  const float ir = 1.0f / rho, irn = 1.0f / rhon;
-  const float P = (rho - S.rho0) * S.k, Pn = rhon * S.kn;
-  dens_b[i] = make_float4(ir, P * ir, irn, Pn * irn);
-  ncount[i] = a.cnt;
-}
-
-// Cell tiles: each warp takes 32 consecutive slots, finds the cells (runs of
-// equal hash) among them and stages every cell's 27 neighbour buckets once
-// into its shared-memory tile (entries of a different float(hash) become
-// +inf so they fail the distance test; .w carries the slot). Each lane then
-// tests its particle against its cell's staged candidates. Cells whose
-// candidates do not fit the tile walk global memory instead.
-template <int kWarps>
-__global__ void __launch_bounds__(kWarps * 32)
-k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
-          const SceneDev* __restrict__ scenes, const float4* __restrict__ pred,
-          const uint32_t* __restrict__ hash_s,
-          const uint32_t* __restrict__ start, float2* __restrict__ dens_a,
-          float4* __restrict__ dens_b, uint32_t* __restrict__ nbr,
-          uint32_t* __restrict__ ncount, uint32_t nbr_stride, uint32_t nbr_cap,
-          uint32_t tile_cap) {
-  extern __shared__ float4 s_cand_all[];
-  __shared__ uint32_t s_off[kWarps][33];
-  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
-  float4* cand = s_cand_all + w * tile_cap;
-  const NbrSink L{nbr, nbr_stride, nbr_cap};
+// -------------------------------------------------------------- cell table
+// For each cell (its first slot), the 27 runs its particles visit: for
+// offset o the bucket of hash(c)+delta_o holds, sorted by hash, the entries
+// the reference keeps -- those whose float(hash) equals float(hash(c+o))
+// (:346) -- as one contiguous run. Lanes take (cell, offset) pairs of the
+// warp's tile in parallel.
+__global__ void k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
+                             const SceneDev* __restrict__ scenes,
+                             const uint32_t* __restrict__ hash_s,
+                             const uint32_t* __restrict__ cell_first,
+                             const uint32_t* __restrict__ start,
+                             uint2* __restrict__ cell_tab) {
+  const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
     const SceneDev& S = scenes[tile_scene(tile)];
-    const bool live = lane < tile_len(tile);
     const uint32_t i = tile.y + lane;
-    const float4 me = live ? pred[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const uint32_t h = live ? hash_s[i] : 0u;
-    const uint32_t hprev = __shfl_up_sync(kFull, h, 1);
-    const bool leader = live && (lane == 0 || h != hprev);
+    const bool live = lane < tile_len(tile);
+    const bool leader = live && cell_first[i] == i;
     const uint32_t lmask = __ballot_sync(kFull, leader);
-    const int ncell = __popc(lmask);
-    const int mycell = __popc(lmask & ((2u << lane) - 1u)) - 1;
-    const float3 p = make_float3(me.x, me.y, me.z);
-    DensityAcc acc;
-    int c0 = 0;
-    while (c0 < ncell) {
-      // stage cells c0.. while they fit the tile
-      uint32_t used = 0, ovf = 0;
-      int c1 = c0;
-      for (; c1 < ncell; ++c1) {
-        const int Ld = __fns(lmask, 0, c1 + 1);
-        const uint32_t hc = __shfl_sync(kFull, h, Ld);
-        uint32_t b0 = 0, cnt = 0;
-        float hf = 0.0f;
-        if (lane < 27) {
-          const uint32_t hh = hc + c_delta[lane];
-          const uint32_t key = S.base + fastmod(hh, S.fm, S.n);
-          b0 = __ldg(start + key);
-          cnt = __ldg(start + key + 1) - b0;
-          hf = __uint2float_rn(hh);
-        }
-        const uint32_t incl = warp_incl_scan(cnt);
-        const uint32_t m = __shfl_sync(kFull, incl, 31);
-        if (lane == 0) s_off[w][c1 - c0] = used;
-        if (m > tile_cap) {  // this cell alone exceeds the tile
-          ovf |= 1u << (c1 - c0);
-          continue;
-        }
-        if (used + m > tile_cap) break;  // next round
-        float4* dst = cand + used + (incl - cnt);
-        for (uint32_t k = 0; k < cnt; ++k) {
-          float4 q = __ldg(pred + b0 + k);
-          if (q.w != hf) q.x = kInf;
-          q.w = __uint_as_float(b0 + k);
-          dst[k] = q;
-        }
-        used += m;
-      }
-      if (lane == 0) s_off[w][c1 - c0] = used;
-      __syncwarp();
-      if (live && mycell >= c0 && mycell < c1) {
-        const int lc = mycell - c0;
-        if ((ovf >> lc) & 1u) {
-          walk27(S, h, start, pred, [&](uint32_t j, float4 q) {
-            acc.visit(S, p, i, j, q, L);
-          });
-        } else {
-          const uint32_t k0 = s_off[w][lc], k1 = s_off[w][lc + 1];
-#pragma unroll 4
-          for (uint32_t k = k0; k < k1; ++k) {
-            const float4 q = cand[k];
-            acc.visit(S, p, i, __float_as_uint(q.w), q, L);
+    const uint32_t pairs = __popc(lmask) * 27u;
+    for (uint32_t q = lane; q < pairs; q += 32) {
+      const uint32_t c = q / 27u, o = q - c * 27u;
+      const int L = __fns(lmask, 0, static_cast<int>(c) + 1);
+      const uint32_t slot = tile.y + static_cast<uint32_t>(L);
+      const uint32_t hc = __ldg(hash_s + slot);
+      const uint32_t hh = hc + c_delta[o];
+      const uint32_t key = S.base + fastmod(hh, S.fm, S.n);
+      const uint32_t b0 = __ldg(start + key), b1 = __ldg(start + key + 1);
+      const float hf = __uint2float_rn(hh);
+      // The bucket is sorted by hash, so the entries with float(hash) == hf
+      // are one run; a bucket holding a single cell is the common case and
+      // is recognised from its first and last entries.
+      uint32_t first = b1, len = 0;
+      if (b1 > b0) {
+        const float f0 = __uint2float_rn(__ldg(hash_s + b0));
+        const float f1 = __uint2float_rn(__ldg(hash_s + b1 - 1));
+        if (f0 == hf && f1 == hf) {
+          first = b0;
+          len = b1 - b0;
+        } else if (f0 <= hf && hf <= f1) {
+          for (uint32_t u = b0; u < b1; ++u) {
+            const bool eq = __uint2float_rn(__ldg(hash_s + u)) == hf;
+            if (eq && len == 0) first = u;
+            len += eq ? 1u : 0u;
           }
         }
       }
-      __syncwarp();
-      c0 = c1;
+      cell_tab[static_cast<uint64_t>(slot) * 27u + o] = make_uint2(first, len);
     }
-    if (live) density_finish(S, i, acc, dens_a, dens_b, ncount);
+  }
+}
+
+// ----------------------------------------------------------------- density
+// CalculateDensity (:325-365) for one particle (self included) and its
+// neighbour list (dist <= r, self excluded) for the force passes, in two
+// phases. Phase 1 walks the cell's runs with the FMA estimate of d2 and only
+// appends candidates within cut_hi (a 2e-6 superset of the cutoff) to the
+// list. Phase 2 re-reads the ~25 listed pairs, classifies each on the
+// reference's exact d2 (dropping the rare band pairs) and accumulates the
+// kernels; contributions vanish at the cutoff ((r-dist)^2), so the hardware
+// square root serves the kernel value. The self pair contributes (r, r).
+__device__ __forceinline__ void density_pair(const SceneDev& S, float d2,
+                                             float& s2, float& s3) {
+  const float w = S.r - sqrt_approx(d2);
+  const float w2 = w * w;
+  s2 += w2;
+  s3 = fmaf(w2, w, s3);
+}
+
+__global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
+                          const SceneDev* __restrict__ scenes,
+                          const float4* __restrict__ pred,
+                          const uint32_t* __restrict__ cell_first,
+                          const uint2* __restrict__ cell_tab,
+                          float2* __restrict__ dens_a,
+                          float4* __restrict__ dens_b,
+                          uint32_t* __restrict__ nbr,
+                          uint32_t* __restrict__ ncount, uint32_t nbr_stride,
+                          uint32_t nbr_cap) {
+  const uint32_t lane = lane_id();
+  for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
+    const uint2 tile = tiles[t];
+    const SceneDev& S = scenes[tile_scene(tile)];
+    const uint32_t i = tile.y + lane;
+    if (lane >= tile_len(tile)) continue;
+    const float4 me = pred[i];
+    const float3 p = make_float3(me.x, me.y, me.z);
+    const uint32_t cf = cell_first[i];
+    uint32_t* row = nbr + i;
+    // phase 1: candidate list
+    uint32_t cnt = 0;
+    walk_runs(cell_tab, cf, pred, [&](uint32_t j, float4 q) {
+      const float d2f = dist2_fast(q.x - p.x, q.y - p.y, q.z - p.z);
+      if (d2f <= S.cut_hi && j != i) {
+        if (cnt < nbr_cap) row[cnt * nbr_stride] = j;
+        ++cnt;
+      }
+    });
+    // phase 2: exact classification and the density sums
+    float s2 = S.r2, s3 = S.r2 * S.r;  // self: w = r
+    if (cnt <= nbr_cap) {
+      uint32_t kept = 0;
+      for (uint32_t k = 0; k < cnt; ++k) {
+        const uint32_t j = row[k * nbr_stride];
+        const float4 q = __ldg(pred + j);
+        const float d2 = dist2(q.x - p.x, q.y - p.y, q.z - p.z);
+        if (d2 <= S.cut_lt) density_pair(S, d2, s2, s3);
+        if (d2 <= S.cut_le) {
+          if (kept != k) row[kept * nbr_stride] = j;
+          ++kept;
+        }
+      }
+      cnt = kept;
+    } else {
+      // list overflow: sum directly; the force passes walk the runs too
+      walk_runs(cell_tab, cf, pred, [&](uint32_t j, float4 q) {
+        const float d2 = dist2(q.x - p.x, q.y - p.y, q.z - p.z);
+        if (j != i && d2 <= S.cut_lt) density_pair(S, d2, s2, s3);
+      });
+    }
+    const float rho = s2 * S.vol2, rhon = s3 * S.vol3;
+    dens_a[i] = make_float2(rho, rhon);
+    const float ir = 1.0f / rho, irn = 1.0f / rhon;
+    const float P = (rho - S.rho0) * S.k, Pn = rhon * S.kn;
+    dens_b[i] = make_float4(ir, P * ir, irn, Pn * irn);
+    ncount[i] = cnt;
   }
 }
 
 // ---------------------------------------------------------------- pressure
 // CalculatePressureForce (:367-422) over the particle's neighbour list (self
 // excluded, dist <= r). shared/rho_j = 0.5*(Pi*(1/rho_j) + Pj/rho_j); the 0.5
-// is folded into ds2h/ds3h. A list that overflowed falls back to the walk.
+// is folded into ds2h/ds3h. The list is read four entries at a time so the
+// gathers of four neighbours are in flight together. A list that overflowed
+// falls back to the walk of the cell's runs.
 __device__ __forceinline__ void pressure_pair(const SceneDev& S, float3 p,
                                               float Pi, float Pni, float4 q,
                                               float4 b, float3& f) {
@@ -470,11 +459,14 @@ __device__ __forceinline__ void pressure_pair(const SceneDev& S, float3 p,
   }
 }
 
+
+
+template <int kGather>
 __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
                            const SceneDev* __restrict__ scenes,
                            const float4* __restrict__ pred,
-                           const uint32_t* __restrict__ hash_s,
-                           const uint32_t* __restrict__ start,
+                           const uint32_t* __restrict__ cell_first,
+                           const uint2* __restrict__ cell_tab,
                            const float2* __restrict__ dens_a,
                            const float4* __restrict__ dens_b,
                            const uint32_t* __restrict__ nbr,
@@ -497,13 +489,23 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
     const uint32_t cnt = ncount[i];
     if (cnt <= nbr_cap) {
       const uint32_t* row = nbr + i;
-#pragma unroll 2
-      for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t j = __ldg(row + k * nbr_stride);
-        pressure_pair(S, p, Pi, Pni, __ldg(pred + j), __ldg(dens_b + j), f);
+      for (uint32_t k0 = 0; k0 < cnt; k0 += kGather) {
+        uint32_t j[kGather];
+        float4 q[kGather], b[kGather];
+#pragma unroll
+        for (int u = 0; u < kGather; ++u)
+          j[u] = (k0 + u < cnt) ? __ldg(row + (k0 + u) * nbr_stride) : i;
+#pragma unroll
+        for (int u = 0; u < kGather; ++u) {
+          q[u] = __ldg(pred + j[u]);
+          b[u] = __ldg(dens_b + j[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kGather; ++u)
+          if (k0 + u < cnt) pressure_pair(S, p, Pi, Pni, q[u], b[u], f);
       }
     } else {
-      walk27(S, hash_s[i], start, pred, [&](uint32_t j, float4 q) {
+      walk_runs(cell_tab, cell_first[i], pred, [&](uint32_t j, float4 q) {
         if (j == i) return;
         const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
         if (dist2(dx, dy, dz) <= S.cut_le)
@@ -538,10 +540,11 @@ __device__ __forceinline__ void visc_pair(const SceneDev& S, float3 p,
   }
 }
 
+template <int kGather>
 __global__ void k_visc_integrate(
     const uint2* __restrict__ tiles, uint32_t ntiles,
     const SceneDev* __restrict__ scenes, const float4* __restrict__ pred,
-    const uint32_t* __restrict__ hash_s, const uint32_t* __restrict__ start,
+    const uint32_t* __restrict__ cell_first, const uint2* __restrict__ cell_tab,
     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ ncount,
     uint32_t nbr_stride, uint32_t nbr_cap, const float4* __restrict__ velp,
     float4* __restrict__ pos, float4* __restrict__ vel,
@@ -564,13 +567,23 @@ __global__ void k_visc_integrate(
       const uint32_t cnt = ncount[i];
       if (cnt <= nbr_cap) {
         const uint32_t* row = nbr + i;
-#pragma unroll 2
-        for (uint32_t k = 0; k < cnt; ++k) {
-          const uint32_t j = __ldg(row + k * nbr_stride);
-          visc_pair(S, p, vi, __ldg(pred + j), __ldg(velp + j), f);
+        for (uint32_t k0 = 0; k0 < cnt; k0 += kGather) {
+          uint32_t j[kGather];
+          float4 q[kGather], vj[kGather];
+#pragma unroll
+          for (int u = 0; u < kGather; ++u)
+            j[u] = (k0 + u < cnt) ? __ldg(row + (k0 + u) * nbr_stride) : i;
+#pragma unroll
+          for (int u = 0; u < kGather; ++u) {
+            q[u] = __ldg(pred + j[u]);
+            vj[u] = __ldg(velp + j[u]);
+          }
+#pragma unroll
+          for (int u = 0; u < kGather; ++u)
+            if (k0 + u < cnt) visc_pair(S, p, vi, q[u], vj[u], f);
         }
       } else {
-        walk27(S, hash_s[i], start, pred, [&](uint32_t j, float4 q) {
+        walk_runs(cell_tab, cell_first[i], pred, [&](uint32_t j, float4 q) {
           if (j != i) visc_pair(S, p, vi, q, __ldg(velp + j), f);
         });
       }
@@ -709,33 +722,22 @@ cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
   if (new_tiles.n) {
     k_reorder<<<grid_for(new_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
         new_tiles.d, new_tiles.n, c.scenes, c.tmp_hi, c.tmp_src, c.start, c.pos,
-        c.vel, c.pos2, c.vel2, c.pred, c.hash_s, c.dbg_key, c.src_limit,
-        c.status);
+        c.vel, c.pos2, c.vel2, c.pred, c.hash_s, c.cell_first, c.dbg_key,
+        c.src_limit, c.status);
+    k_cell_table<<<grid_for(new_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
+        new_tiles.d, new_tiles.n, c.scenes, c.hash_s, c.cell_first, c.start,
+        c.cell_tab);
   }
   return cudaGetLastError();
-}
-
-constexpr int kDensityWarps = 4;
-
-size_t density_smem_bytes(int tile_cap) {
-  return static_cast<size_t>(kDensityWarps) * tile_cap * sizeof(float4);
-}
-
-cudaError_t density_configure(int tile_cap) {
-  return cudaFuncSetAttribute(k_density<kDensityWarps>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(density_smem_bytes(tile_cap)));
 }
 
 cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
                            cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
-  const int b = kDensityWarps * 32;
-  k_density<kDensityWarps><<<grid_for(tiles.n, b, c.max_blocks), b,
-                             density_smem_bytes(c.tile_cap), st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.hash_s, c.start, c.dens_a,
-      c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap,
-      static_cast<uint32_t>(c.tile_cap));
+  const int b = c.block_nbr;
+  k_density<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
+      tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.dens_a,
+      c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap);
   return cudaGetLastError();
 }
 
@@ -743,8 +745,10 @@ cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
                             cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_nbr;
-  k_pressure<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.hash_s, c.start, c.dens_a,
+  auto kern = c.gather == 2 ? k_pressure<2> : c.gather == 8 ? k_pressure<8>
+                                                           : k_pressure<4>;
+  kern<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
+      tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.dens_a,
       c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap, c.vel2, c.velp,
       c.dbg_accp);
   return cudaGetLastError();
@@ -755,9 +759,12 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                                   cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_nbr;
-  k_visc_integrate<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.hash_s, c.start, c.nbr, c.ncount,
-      c.nbr_stride, c.nbr_cap, c.velp, c.pos2, c.vel2,
+  auto kern = c.gather == 2   ? k_visc_integrate<2>
+              : c.gather == 8 ? k_visc_integrate<8>
+                              : k_visc_integrate<4>;
+  kern<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
+      tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.nbr,
+      c.ncount, c.nbr_stride, c.nbr_cap, c.velp, c.pos2, c.vel2,
       write_out ? c.out4 : nullptr, fuse_next, c.count, c.keyrank, c.dbg_velv,
       c.status);
   return cudaGetLastError();

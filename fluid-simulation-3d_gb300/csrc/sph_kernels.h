@@ -51,6 +51,8 @@ struct LaunchCtx {
   uint2* tmp_hi = nullptr;    // (hash, id) per bucketed slot
   uint32_t* tmp_src = nullptr;  // source slot per bucketed slot
   uint32_t* hash_s = nullptr;   // cell hash per sorted slot
+  uint32_t* cell_first = nullptr;  // first slot of the particle's cell
+  uint2* cell_tab = nullptr;    // per cell (first slot): 27 (first, len) runs
   uint32_t* count = nullptr;
   uint32_t* start = nullptr;
   uint32_t* partial = nullptr;
@@ -58,7 +60,7 @@ struct LaunchCtx {
   uint32_t* ncount = nullptr;   // neighbours per slot (> nbr_cap: overflow)
   uint32_t nbr_stride = 0;
   uint32_t nbr_cap = 0;
-  int tile_cap = 1024;          // candidates per warp's shared-memory tile
+  int gather = 4;               // neighbour entries gathered per batch (2, 4, 8)
   float4* out4 = nullptr;
   uint32_t* status = nullptr;
   uint32_t* dbg_key = nullptr;
@@ -85,10 +87,6 @@ cudaError_t launch_scan(const LaunchCtx& c, uint32_t len, cudaStream_t st);
 cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
                                 const Tiles& new_tiles, uint32_t total,
                                 cudaStream_t st);
-// Dynamic shared memory of the density kernel for a given tile capacity;
-// density_configure raises the kernel's shared-memory limit accordingly.
-size_t density_smem_bytes(int tile_cap);
-cudaError_t density_configure(int tile_cap);
 cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
                            cudaStream_t st);
 cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
@@ -97,10 +95,10 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                                   int fuse_next, int write_out,
                                   cudaStream_t st);
 
-// Kernels launched by one substep (scan 3, scatter, reorder, density,
-// pressure, viscosity) and by the standalone prediction of a step's first
-// substep.
-constexpr int kKernelsPerSubstep = 8;
+// Kernels launched by one substep (scan 3, scatter, reorder, cell table,
+// density, pressure, viscosity) and by the standalone prediction of a
+// step's first substep.
+constexpr int kKernelsPerSubstep = 9;
 constexpr int kKernelsPredict = 1;
 cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
                           const float4* vel, const float2* dens, float* opos,

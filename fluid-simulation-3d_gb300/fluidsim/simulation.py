@@ -378,7 +378,7 @@ class Batch:
                                                  _ptr(dens), self._stream))
         return pos, vel, dens
 
-    def set_tuning(self, block=128, cell_tile=1024, particles_per_warp=32):
+    def set_tuning(self, block=128, cell_tile=4, particles_per_warp=32):
         t = Tuning(block, cell_tile, particles_per_warp)
         self._check(self._lib.sph_batch_set_tuning(self._h, ctypes.byref(t)))
 
