@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
     ap.add_argument("--workload", default="dam_break_1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
     return ap.parse_args()
 
@@ -227,6 +228,10 @@ def run_native(args):
     stream = torch.cuda.current_stream()
     sim = fluidsim.FluidSimulation(sc["params"], stream=stream)
     sim.InitializeData(n, sc["pos"], sc["vel"])
+    tuning = None
+    if not args.no_autotune:
+        tuning, tuned_ms = sim.autotune(dt, S, steps_per_trial=2)
+        sim.upload(sc["pos"], sc["vel"])  # timed steps start from the scene
     sim.profile_enable(True)
 
     for _ in range(args.warmup):
@@ -290,6 +295,7 @@ def run_native(args):
         tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e_value = world * n * e2e_steps / e2e_s
+    sim_tuning = sim.tuning()
     sim.close()
 
     if rank != 0:
@@ -317,7 +323,8 @@ def run_native(args):
         "dtype": "f32", "data": "synthetic (seeded dam-break lattice, no dataset)",
         "config": {"workload": args.workload, "particles": n, "substeps": S,
                    "dt": dt, "parallelism": f"replicas{world}" if world > 1 else "single",
-                   "l2": "flushed (256 MiB write) before every timed step"},
+                   "l2": "flushed (256 MiB write) before every timed step",
+                   "tuning": tuning or sim_tuning},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -164,6 +164,25 @@ int sph_phase_times(sph_sim* sim, double out_ms[6]) {
   return sim->eng.PhaseTimes(out_ms);
 }
 
+int sph_set_tuning(sph_sim* sim, const sph_tuning* t) {
+  if (!sim || !t) return SPH_ERR_INVALID;
+  return sim->eng.SetTuning(*t);
+}
+
+int sph_get_tuning(const sph_sim* sim, sph_tuning* t) {
+  if (!sim || !t) return SPH_ERR_INVALID;
+  *t = sim->eng.Tuning();
+  return SPH_OK;
+}
+
+int sph_autotune(sph_sim* sim, float dt, int substeps, int steps_per_trial,
+                 sph_tuning* best, float* best_ms, void* stream) {
+  if (!sim) return SPH_ERR_INVALID;
+  const int rc = sim->eng.SetDt(sim->scene, dt);
+  if (rc != SPH_OK) return rc;
+  return sim->eng.Autotune(substeps, steps_per_trial, best, best_ms, S(stream));
+}
+
 uint64_t sph_kernel_launches(const sph_sim* sim) {
   return sim ? sim->eng.KernelLaunches() : 0;
 }

@@ -39,8 +39,7 @@ SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base,
   d.cut_lt = std::min(p.cutoff_sq, t_lt);
   d.cut_le = std::min(p.cutoff_sq, t_le);
   d.cut_hi = d.cut_le * 1.000002f;
-  d.cut_lo = d.cut_lt * 0.999998f;
-  d.r2 = r * r;
+  d.cut_lo = d.cut_lt * 0.999998f;  d.r2 = r * r;
   // kernels.h:28,40,52,64,76 -- same float expressions.
   d.vol2 = 15.0f / (2.0f * kPiF * powf(r, 5.0f));
   d.vol3 = 15.0f / (kPiF * powf(r, 6.0f));
@@ -345,7 +344,7 @@ int Engine::UploadScenes(int substeps, cudaStream_t st) {
 int Engine::RunSubsteps(int substeps, cudaStream_t st) {
   LaunchCtx c = ctx_;
   c.block_nbr = tuning_.block;
-  c.gather = tuning_.cell_tile;
+  c.cell_tile = tuning_.cell_tile;
   c.max_blocks = 0;
   c.src_limit = static_cast<uint32_t>(capacity_);
   int cur = cur_;
@@ -642,8 +641,9 @@ int Engine::SetTuning(const sph_tuning& t) {
     return Fail(SPH_ERR_INVALID, "block must be a multiple of 32 in [32, 1024]");
   if (t.particles_per_warp != 32)
     return Fail(SPH_ERR_INVALID, "particles_per_warp must be 32");
-  if (t.cell_tile != 2 && t.cell_tile != 4 && t.cell_tile != 8)
-    return Fail(SPH_ERR_INVALID, "cell_tile must be 2, 4 or 8");
+  if (t.cell_tile != 1 && t.cell_tile != 64 && t.cell_tile != 128 &&
+      t.cell_tile != 192 && t.cell_tile != 256)
+    return Fail(SPH_ERR_INVALID, "cell_tile must be 1, 64, 128, 192 or 256");
   if (t.block != tuning_.block || t.particles_per_warp != tuning_.particles_per_warp ||
       t.cell_tile != tuning_.cell_tile)
     ReleaseGraphs();
@@ -656,7 +656,7 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
   if (steps_per_trial < 1) return Fail(SPH_ERR_INVALID, "steps_per_trial >= 1");
   std::vector<sph_tuning> space;
   for (int b : {64, 128, 256, 512})
-    for (int tile : {2, 4, 8}) space.push_back(sph_tuning{b, tile, 32});
+    for (int tile : {1, 64, 128, 256}) space.push_back(sph_tuning{b, tile, 32});
   sph_tuning win = tuning_;
   float win_ms = std::numeric_limits<float>::infinity();
   cudaEvent_t e0, e1;

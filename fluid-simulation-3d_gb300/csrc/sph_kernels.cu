@@ -373,6 +373,75 @@ __device__ __forceinline__ void density_pair(const SceneDev& S, float d2,
   s3 = fmaf(w2, w, s3);
 }
 
+__device__ __forceinline__ void density_store(const SceneDev& S, uint32_t i,
+                                              float s2, float s3, uint32_t cnt,
+                                              float2* __restrict__ dens_a,
+                                              float4* __restrict__ dens_b,
+                                              uint32_t* __restrict__ ncount) {
+  const float rho = s2 * S.vol2, rhon = s3 * S.vol3;
+  dens_a[i] = make_float2(rho, rhon);
+  const float ir = 1.0f / rho, irn = 1.0f / rhon;
+  const float P = (rho - S.rho0) * S.k, Pn = rhon * S.kn;
+  dens_b[i] = make_float4(ir, P * ir, irn, Pn * irn);
+  ncount[i] = cnt;
+}
+
+// Thread-per-particle form in one pass: each lane walks its cell's runs,
+// classifies every candidate (FMA estimate, exact d2 inside the 2e-6 band)
+// and accumulates the density and its list as it goes. Lanes of one cell
+// walk identical runs, so their loads coincide.
+__global__ void k_density_walk(const uint2* __restrict__ tiles,
+                               uint32_t ntiles,
+                               const SceneDev* __restrict__ scenes,
+                               const float4* __restrict__ pred,
+                               const uint32_t* __restrict__ cell_first,
+                               const uint2* __restrict__ cell_tab,
+                               float2* __restrict__ dens_a,
+                               float4* __restrict__ dens_b,
+                               uint32_t* __restrict__ nbr,
+                               uint32_t* __restrict__ ncount,
+                               uint32_t nbr_stride, uint32_t nbr_cap) {
+  const uint32_t lane = lane_id();
+  for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
+    const uint2 tile = tiles[t];
+    const SceneDev& S = scenes[tile_scene(tile)];
+    if (lane >= tile_len(tile)) continue;
+    const uint32_t i = tile.y + lane;
+    const float4 me = pred[i];
+    const float3 p = make_float3(me.x, me.y, me.z);
+    uint32_t* row = nbr + i;
+    float s2 = S.r2, s3 = S.r2 * S.r;  // self: w = r
+    uint32_t cnt = 0;
+    walk_runs(cell_tab, cell_first[i], pred, [&](uint32_t j, float4 q) {
+      const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+      const float d2f = dist2_fast(dx, dy, dz);
+      if (d2f <= S.cut_hi && j != i) {
+        bool in_lt = true, in_le = true;
+        if (d2f > S.cut_lo) {
+          const float d2 = dist2(dx, dy, dz);
+          in_lt = d2 <= S.cut_lt;
+          in_le = d2 <= S.cut_le;
+        }
+        if (in_le) {
+          if (cnt < nbr_cap) row[cnt * nbr_stride] = j;
+          ++cnt;
+        }
+        if (in_lt) density_pair(S, d2f, s2, s3);
+      }
+    });
+    density_store(S, i, s2, s3, cnt, dens_a, dens_b, ncount);
+  }
+}
+
+// Phase 1 is warp-cooperative over the cells of the warp's 32 slots: for
+// each cell, lanes 0..26 fetch its 27 runs, a warp scan gives their offsets
+// in the cell's flat candidate sequence, and each lane holds kChunks of those
+// candidates in registers (its slot found by a shuffle binary search over
+// the run offsets) -- a cell tile of kChunks*32 candidates. Every particle of
+// the cell is then tested against the whole tile at once: one ballot per 32
+// pairs appends the hits to that particle's list. Longer candidate sequences
+// are processed tile by tile.
+template <int kChunks>
 __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
                           const SceneDev* __restrict__ scenes,
                           const float4* __restrict__ pred,
@@ -384,24 +453,75 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
                           uint32_t* __restrict__ ncount, uint32_t nbr_stride,
                           uint32_t nbr_cap) {
   const uint32_t lane = lane_id();
+  const uint32_t lt_mask = (1u << lane) - 1u;
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
     const SceneDev& S = scenes[tile_scene(tile)];
     const uint32_t i = tile.y + lane;
-    if (lane >= tile_len(tile)) continue;
-    const float4 me = pred[i];
-    const float3 p = make_float3(me.x, me.y, me.z);
-    const uint32_t cf = cell_first[i];
-    uint32_t* row = nbr + i;
-    // phase 1: candidate list
-    uint32_t cnt = 0;
-    walk_runs(cell_tab, cf, pred, [&](uint32_t j, float4 q) {
-      const float d2f = dist2_fast(q.x - p.x, q.y - p.y, q.z - p.z);
-      if (d2f <= S.cut_hi && j != i) {
-        if (cnt < nbr_cap) row[cnt * nbr_stride] = j;
-        ++cnt;
+    const bool live = lane < tile_len(tile);
+    const float4 me = live ? pred[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t cf = live ? cell_first[i] : 0xffffffffu;
+    const uint32_t cf_prev = __shfl_up_sync(kFull, cf, 1);
+    const uint32_t lead = __ballot_sync(kFull, live && (lane == 0 || cf != cf_prev));
+    const uint32_t live_end = tile_len(tile);
+    // phase 1: candidate lists (FMA estimate of d2 within cut_hi)
+    uint32_t cnt = 0;  // list length of this lane's particle
+    for (uint32_t cells = lead; cells != 0;) {
+      const int c0 = __ffs(cells) - 1;
+      cells &= cells - 1;
+      const int c1 = cells ? __ffs(cells) - 1 : static_cast<int>(live_end);
+      const uint32_t cfc = __shfl_sync(kFull, cf, c0);
+      uint2 run = make_uint2(0u, 0u);
+      if (lane < 27) run = __ldg(cell_tab + static_cast<uint64_t>(cfc) * 27u + lane);
+      const uint32_t incl = warp_incl_scan(run.y);
+      const uint32_t excl = incl - run.y;
+      const uint32_t total = __shfl_sync(kFull, incl, 31);
+      for (uint32_t seg = 0; seg < total; seg += kChunks * 32u) {
+        float4 q[kChunks];
+        uint32_t js[kChunks];
+#pragma unroll
+        for (int c = 0; c < kChunks; ++c) {
+          const uint32_t e = seg + c * 32u + lane;
+          // o = number of runs ending at or before e (incl is ascending)
+          uint32_t o = 0;
+#pragma unroll
+          for (uint32_t step = 16; step >= 1; step >>= 1) {
+            const uint32_t probe = o + step - 1u;
+            const uint32_t v = __shfl_sync(kFull, incl, probe < 27u ? probe : 26u);
+            if (probe < 27u && v <= e) o += step;
+          }
+          const uint32_t src = o < 27u ? o : 26u;
+          const uint32_t rx = __shfl_sync(kFull, run.x, src);
+          const uint32_t rex = __shfl_sync(kFull, excl, src);
+          js[c] = rx + (e - rex);
+          q[c] = e < total ? __ldg(pred + js[c])
+                           : make_float4(__int_as_float(0x7f800000), 0.f, 0.f, 0.f);
+        }
+        for (int pp = c0; pp < c1; ++pp) {
+          const float px = __shfl_sync(kFull, me.x, pp);
+          const float py = __shfl_sync(kFull, me.y, pp);
+          const float pz = __shfl_sync(kFull, me.z, pp);
+          const uint32_t ip = tile.y + static_cast<uint32_t>(pp);
+          uint32_t base = __shfl_sync(kFull, cnt, pp);
+#pragma unroll
+          for (int c = 0; c < kChunks; ++c) {
+            if (seg + c * 32u >= total) break;
+            const float d2f = dist2_fast(q[c].x - px, q[c].y - py, q[c].z - pz);
+            const bool hit = d2f <= S.cut_hi && js[c] != ip;
+            const uint32_t hm = __ballot_sync(kFull, hit);
+            if (hit) {
+              const uint32_t k = base + __popc(hm & lt_mask);
+              if (k < nbr_cap) nbr[k * nbr_stride + ip] = js[c];
+            }
+            base += __popc(hm);
+          }
+          if (lane == static_cast<uint32_t>(pp)) cnt = base;
+        }
       }
-    });
+    }
+    if (!live) continue;
+    const float3 p = make_float3(me.x, me.y, me.z);
+    uint32_t* row = nbr + i;
     // phase 2: exact classification and the density sums
     float s2 = S.r2, s3 = S.r2 * S.r;  // self: w = r
     if (cnt <= nbr_cap) {
@@ -479,8 +599,8 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
     const SceneDev& S = scenes[tile_scene(tile)];
-    const uint32_t i = tile.y + lane;
     if (lane >= tile_len(tile)) continue;
+    const uint32_t i = tile.y + lane;
     const float4 pi = pred[i];
     const float3 p = make_float3(pi.x, pi.y, pi.z);
     const float2 di = dens_a[i];
@@ -555,8 +675,8 @@ __global__ void k_visc_integrate(
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
     const SceneDev& S = scenes[tile_scene(tile)];
-    const uint32_t i = tile.y + lane;
     const bool live = lane < tile_len(tile);
+    const uint32_t i = tile.y + lane;
     bool bad = false;
     uint32_t key = 0, hash = 0, id = 0;
     if (live) {
@@ -735,7 +855,19 @@ cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
                            cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_nbr;
-  k_density<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
+  const uint32_t g = grid_for(tiles.n, b, c.max_blocks);
+  if (c.cell_tile <= 1) {
+    k_density_walk<<<g, b, 0, st>>>(tiles.d, tiles.n, c.scenes, c.pred,
+                                    c.cell_first, c.cell_tab, c.dens_a,
+                                    c.dens_b, c.nbr, c.ncount, c.nbr_stride,
+                                    c.nbr_cap);
+    return cudaGetLastError();
+  }
+  auto kern = c.cell_tile <= 64    ? k_density<2>
+              : c.cell_tile <= 128 ? k_density<4>
+              : c.cell_tile <= 192 ? k_density<6>
+                                   : k_density<8>;
+  kern<<<g, b, 0, st>>>(
       tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.dens_a,
       c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap);
   return cudaGetLastError();

@@ -61,6 +61,8 @@ struct LaunchCtx {
   uint32_t nbr_stride = 0;
   uint32_t nbr_cap = 0;
   int gather = 4;               // neighbour entries gathered per batch (2, 4, 8)
+  int cell_tile = 1;            // density-pass candidates held per cell tile
+                                // (1: thread-per-particle walk)
   float4* out4 = nullptr;
   uint32_t* status = nullptr;
   uint32_t* dbg_key = nullptr;

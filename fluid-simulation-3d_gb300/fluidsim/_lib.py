@@ -29,7 +29,8 @@ EXPORTS = (
     "sph_batch_autotune", "sph_batch_num_scenes", "sph_batch_num_particles",
     "sph_batch_last_error", "sph_profile_enable", "sph_phase_times",
     "sph_kernel_launches", "sph_batch_kernel_launches",
-    "sph_batch_profile_enable", "sph_batch_phase_times",
+    "sph_batch_profile_enable", "sph_batch_phase_times", "sph_set_tuning",
+    "sph_get_tuning", "sph_autotune",
 )
 
 
@@ -101,6 +102,10 @@ def _sig(L):
         "sph_batch_kernel_launches": (u64, [_P]),
         "sph_batch_profile_enable": (i, [_P, i]),
         "sph_batch_phase_times": (i, [_P, ctypes.POINTER(ctypes.c_double)]),
+        "sph_set_tuning": (i, [_P, ctypes.POINTER(Tuning)]),
+        "sph_get_tuning": (i, [_P, ctypes.POINTER(Tuning)]),
+        "sph_autotune": (i, [_P, f, i, i, ctypes.POINTER(Tuning),
+                             ctypes.POINTER(f), _P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

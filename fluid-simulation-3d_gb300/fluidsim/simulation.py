@@ -204,6 +204,28 @@ class FluidSimulation:
     def kernel_launches(self) -> int:
         return int(self._lib.sph_kernel_launches(self._h))
 
+    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32):
+        t = Tuning(block, cell_tile, particles_per_warp)
+        check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), self._h)
+
+    def tuning(self):
+        t = Tuning()
+        check(self._lib.sph_get_tuning(self._h, ctypes.byref(t)), self._h)
+        return dict(block=t.block, cell_tile=t.cell_tile,
+                    particles_per_warp=t.particles_per_warp)
+
+    def autotune(self, deltatime, substeps=1, steps_per_trial=2):
+        """Sweep the launch configuration on real steps (the state advances);
+        keeps the fastest. Returns (tuning dict, ms per step)."""
+        t = Tuning()
+        ms = ctypes.c_float()
+        check(self._lib.sph_autotune(self._h, _f32(deltatime), int(substeps),
+                                     int(steps_per_trial), ctypes.byref(t),
+                                     ctypes.byref(ms), self._stream), self._h)
+        self._cache = None
+        return dict(block=t.block, cell_tile=t.cell_tile,
+                    particles_per_warp=t.particles_per_warp), float(ms.value)
+
     @property
     def handle(self):
         return self._h
@@ -378,7 +400,7 @@ class Batch:
                                                  _ptr(dens), self._stream))
         return pos, vel, dens
 
-    def set_tuning(self, block=128, cell_tile=4, particles_per_warp=32):
+    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32):
         t = Tuning(block, cell_tile, particles_per_warp)
         self._check(self._lib.sph_batch_set_tuning(self._h, ctypes.byref(t)))
 

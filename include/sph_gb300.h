@@ -57,6 +57,17 @@ typedef struct sph_params {
 
 typedef struct sph_sim sph_sim;
 
+/* Launch configuration of the neighbour kernels, chosen by the autotuner
+ * (sph_autotune / sph_batch_autotune) by timing real steps. */
+typedef struct sph_tuning {
+  int32_t block;      /* threads per block of the neighbour kernels
+                         (multiple of 32, 32..1024), default 128          */
+  int32_t cell_tile;  /* candidates of a cell held in a warp's registers
+                         per pass of the density kernel: 64, 128, 192 or
+                         256 (default 128)                                */
+  int32_t particles_per_warp; /* particles per warp: 32 (one per lane)    */
+} sph_tuning;
+
 /* Reference defaults of physicsWorld.h:96-106,145 and physicsWorld.cc:47,87. */
 void sph_default_params(sph_params *out);
 
@@ -136,6 +147,15 @@ int sph_status(sph_sim *sim, uint32_t *flags, void *stream);
 int sph_profile_enable(sph_sim *sim, int enable);
 int sph_phase_times(sph_sim *sim, double out_ms[6]);
 
+/* Kernel launch configuration of a single-scene handle, and its autotuner:
+ * sweeps block size and gather batch on real steps of dt/substeps (the state
+ * advances by steps_per_trial + 1 steps per candidate), keeps the fastest
+ * and reports it (best may be NULL) with its ms per step. */
+int sph_set_tuning(sph_sim *sim, const sph_tuning *t);
+int sph_get_tuning(const sph_sim *sim, sph_tuning *t);
+int sph_autotune(sph_sim *sim, float dt, int substeps, int steps_per_trial,
+                 sph_tuning *best, float *best_ms, void *stream);
+
 /* Number of this library's kernels the handle has launched so far
  * (including those replayed from captured graphs). */
 uint64_t sph_kernel_launches(const sph_sim *sim);
@@ -178,15 +198,8 @@ int sph_batch_step(sph_batch *b, int substeps, void *stream);
 int sph_batch_download(sph_batch *b, uint32_t scene_id, float *pos3,
                        float *vel3, float *dens2, void *stream);
 
-/* Launch configuration of the neighbour kernels and the autotuner that picks
- * it by timing the current scene set (block size, cell-tile size and
- * particles per warp; see sph_tuning). */
-typedef struct sph_tuning {
-  int32_t block;           /* threads per block of the neighbour kernels */
-  int32_t cell_tile;       /* candidate slots staged per tile             */
-  int32_t particles_per_warp; /* 32 = one particle per lane; 8/16 = lanes
-                                 split each particle's candidates         */
-} sph_tuning;
+/* Launch configuration of the batch's neighbour kernels and its autotuner
+ * (see sph_tuning above). */
 int sph_batch_set_tuning(sph_batch *b, const sph_tuning *t);
 int sph_batch_get_tuning(const sph_batch *b, sph_tuning *t);
 /* Sweep the tuning space on the resident scenes (runs real steps, so the
