@@ -30,8 +30,10 @@ EXPORTS = (
     "sph_batch_last_error", "sph_profile_enable", "sph_phase_times",
     "sph_kernel_launches", "sph_batch_kernel_launches",
     "sph_batch_profile_enable", "sph_batch_phase_times", "sph_set_tuning",
-    "sph_get_tuning", "sph_autotune",
+    "sph_get_tuning", "sph_autotune", "sph_spatial_lookup_static",
+    "sph_static_error",
 )
+STATIC_LOOKUP_MAX = 65536
 
 
 class Params(ctypes.Structure):
@@ -106,6 +108,8 @@ def _sig(L):
         "sph_get_tuning": (i, [_P, ctypes.POINTER(Tuning)]),
         "sph_autotune": (i, [_P, f, i, i, ctypes.POINTER(Tuning),
                              ctypes.POINTER(f), _P]),
+        "sph_spatial_lookup_static": (i, [_P, u32, f, _P, _P, _P, _P, _P]),
+        "sph_static_error": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

@@ -167,6 +167,37 @@ const char *sph_last_error(const sph_sim *sim);
 const char *sph_global_error(void);
 
 /* ------------------------------------------------------------------------
+ * Spatial lookup without device allocation. No counterpart in the
+ * reference: this is an extra entry point for callers that cannot allocate
+ * device memory -- a render loop that must not stall a frame on cudaMalloc's
+ * device-wide synchronisation, an engine that owns a fixed memory pool and
+ * forbids plug-ins to allocate, code running inside another library's
+ * captured or stream-ordered region.
+ *
+ * Builds, for n predicted positions (device float[3n], the caller's
+ * buffers), the same lookup as the main path: hash[n] and key[n] = hash % n
+ * per particle, sorted_ids[n] in (key, index) order and start[n]
+ * (0x7fffffff for an empty key) -- all device buffers of the caller. The
+ * working memory is one array inside the library of 16 B per particle for
+ * at most SPH_STATIC_LOOKUP_MAX particles (1 MiB, held on every GPU that
+ * loads the library until the process exits); larger n is rejected with
+ * SPH_ERR_INVALID. Nothing is allocated: no cudaMalloc/cudaFree or
+ * allocating library call. The first call on a device resolves that array's
+ * address (cudaGetSymbolAddress) with the device current, so make the first
+ * call on each device before any stream capture. Each device has its own
+ * copy of the array and every call on that device shares it, keeping the
+ * last call's contents (each call clears what must start at zero): two calls
+ * whose work overlaps on the same GPU, e.g. on different streams, race, so
+ * serialise them (one stream does). Asynchronous on `stream`; the message of
+ * the last failure is sph_static_error(). */
+#define SPH_STATIC_LOOKUP_MAX 65536u
+int sph_spatial_lookup_static(const float *dpred3, uint32_t n, float radius,
+                              uint32_t *dhash, uint32_t *dkey,
+                              uint32_t *dsorted_ids, uint32_t *dstart,
+                              void *stream);
+const char *sph_static_error(void);
+
+/* ------------------------------------------------------------------------
  * Batched form: many independent scenes of uneven sizes advanced together.
  * Each kernel of a substep is one segmented, persistent launch over all
  * scenes; a whole step is captured once in a CUDA graph and replayed.
