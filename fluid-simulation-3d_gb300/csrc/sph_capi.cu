@@ -224,6 +224,12 @@ int sph_batch_remove(sph_batch* b, uint32_t scene_id) {
   return b->eng.RemoveScene(scene_id);
 }
 
+int sph_batch_sync(sph_batch* b, void* stream) {
+  if (!b) return SPH_ERR_INVALID;
+  const cudaError_t e = cudaStreamSynchronize(S(stream));
+  return e == cudaSuccess ? SPH_OK : b->eng.CudaFail(e, "cudaStreamSynchronize");
+}
+
 int sph_batch_step(sph_batch* b, int substeps, void* stream) {
   if (!b) return SPH_ERR_INVALID;
   return b->eng.Step(substeps, S(stream));
@@ -251,6 +257,8 @@ int sph_batch_autotune(sph_batch* b, int substeps, int steps_per_trial,
   if (!b) return SPH_ERR_INVALID;
   return b->eng.Autotune(substeps, steps_per_trial, best, best_ms, S(stream));
 }
+
+uint64_t sph_bytes_per_particle(void) { return sph::Engine::BytesPerParticle(); }
 
 uint32_t sph_batch_num_scenes(const sph_batch* b) {
   return b ? b->eng.NumScenes() : 0;

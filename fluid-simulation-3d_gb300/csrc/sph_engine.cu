@@ -168,6 +168,20 @@ int Engine::Init() {
   return SPH_OK;
 }
 
+uint64_t Engine::BytesPerParticle() {
+  return 2 * 2 * sizeof(float4)                // pos, vel (double-buffered)
+         + 2 * sizeof(float4)                  // pred, velp
+         + sizeof(float2) + sizeof(float4)     // dens_a, dens_b
+         + sizeof(uint4)                       // keyrank
+         + sizeof(uint2) + 4 * sizeof(uint32_t)  // tmp_hi, tmp_src, hash_s,
+                                                 // cell_first, ncount
+         + 27 * sizeof(uint2)                  // cell_tab
+         + kNbrCap * sizeof(uint32_t)          // nbr
+         + 2 * sizeof(uint32_t)                // count, start
+         + sizeof(float4)                      // out4
+         + sizeof(uint2);                      // tiles (old + new, per 32)
+}
+
 uint32_t Engine::NumScenes() const {
   uint32_t c = 0;
   for (const auto& s : scenes_) c += s.live ? 1 : 0;

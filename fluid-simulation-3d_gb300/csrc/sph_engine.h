@@ -54,6 +54,8 @@ class Engine {
   int ProfileEnable(bool on);
   int PhaseTimes(double out_ms[6]);
   uint64_t KernelLaunches() const { return launches_; }
+  // Device bytes allocated per particle of capacity (Init's per-C arrays).
+  static uint64_t BytesPerParticle();
 
   void UseGraphs(bool on) { use_graphs_ = on; }
   uint32_t NumScenes() const;

@@ -31,7 +31,7 @@ EXPORTS = (
     "sph_kernel_launches", "sph_batch_kernel_launches",
     "sph_batch_profile_enable", "sph_batch_phase_times", "sph_set_tuning",
     "sph_get_tuning", "sph_autotune", "sph_spatial_lookup_static",
-    "sph_static_error",
+    "sph_static_error", "sph_bytes_per_particle", "sph_batch_sync",
 )
 STATIC_LOOKUP_MAX = 65536
 
@@ -110,6 +110,8 @@ def _sig(L):
                              ctypes.POINTER(f), _P]),
         "sph_spatial_lookup_static": (i, [_P, u32, f, _P, _P, _P, _P, _P]),
         "sph_static_error": (ctypes.c_char_p, []),
+        "sph_bytes_per_particle": (u64, []),
+        "sph_batch_sync": (i, [_P, _P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

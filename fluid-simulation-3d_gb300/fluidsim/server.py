@@ -1,0 +1,162 @@
+"""Serving form: a continuous-batching request loop over the batched engine.
+
+Requests (a scene of N particles to advance K steps) arrive over time. The
+loop admits them, first come first served, with smaller later requests
+allowed to backfill. A request is admitted while the HBM state budget
+(capacity = budget / device bytes per particle) and the scene slots have
+room. Admitted state stays resident on the device, and every resident scene
+advances one step per batched launch, so requests that arrive while others
+run share the device with them. A request leaves, with its final state read
+back, after its K-th step. The loop records each request's per-step
+latency: the wall time of the batched step it took part in, measured with a
+stream sync around the step.
+
+The batched step runs the same per-particle arithmetic in the same order as a
+scene stepped alone, so every result is the same alone and in the mix (the
+GPU tests check it bit for bit).
+"""
+from __future__ import annotations
+
+import dataclasses
+import time
+
+import numpy as np
+
+from . import _lib
+from .simulation import Batch, FluidSimulation
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    params: object
+    pos: np.ndarray
+    vel: np.ndarray
+    dt: float
+    substeps: int
+    steps: int
+    arrival: float = 0.0  # seconds after the loop starts
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+
+@dataclasses.dataclass
+class Done:
+    rid: int
+    pos: np.ndarray
+    vel: np.ndarray
+    dens: np.ndarray
+    admitted: float
+    finished: float
+    step_ms: list
+
+
+def bytes_per_particle() -> int:
+    return int(_lib.load().sph_bytes_per_particle())
+
+
+class Server:
+    """Continuous batching under an HBM budget (bytes of resident state)."""
+
+    def __init__(self, budget_bytes: int, max_scenes: int = 4096, stream=None,
+                 tuning=None):
+        self.capacity = max(1, int(budget_bytes) // bytes_per_particle())
+        self.batch = Batch(self.capacity, max_scenes, stream)
+        if tuning:
+            self.batch.set_tuning(**tuning)
+        self.resident = {}  # scene id -> [request, steps left, admitted, step_ms]
+
+    def close(self):
+        self.batch.close()
+
+    def _admit(self, waiting, now):
+        admitted = []
+        for req in list(waiting):
+            sid = self.batch.try_add(req.params, req.pos, req.vel, req.dt)
+            if sid is None:
+                continue  # does not fit now; a smaller later one may
+            self.resident[sid] = [req, req.steps, now, []]
+            waiting.remove(req)
+            admitted.append(req.rid)
+        return admitted
+
+    def run(self, requests, realtime=True, on_step=None):
+        """Serve `requests` (sorted by arrival). Returns (results by rid,
+        stats dict). With realtime the loop waits for arrivals on the wall
+        clock; otherwise time jumps to the next arrival when idle."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        substeps = {r.substeps for r in pending}
+        if len(substeps) > 1:
+            raise ValueError("one substep count per server")
+        substeps = substeps.pop() if substeps else 1
+        waiting, done = [], {}
+        t0 = time.perf_counter()
+        offset = 0.0  # time skipped while idle (realtime=False)
+        lat, steps, pstep = [], 0, 0
+        peak_resident = 0
+        while pending or waiting or self.resident:
+            now = time.perf_counter() - t0 + offset
+            while pending and pending[0].arrival <= now:
+                waiting.append(pending.pop(0))
+            self._admit(waiting, now)
+            if not self.resident:
+                if pending:
+                    gap = pending[0].arrival - now
+                    if realtime:
+                        time.sleep(max(0.0, gap))
+                    else:
+                        offset += max(0.0, gap)
+                    continue
+                if waiting:
+                    raise RuntimeError(f"request {waiting[0].rid} ({waiting[0].n} particles) "
+                                       f"exceeds the capacity of {self.capacity}")
+                break
+            peak_resident = max(peak_resident, sum(v[0].n for v in self.resident.values()))
+            ts = time.perf_counter()
+            self.batch.step(substeps)
+            self.batch.sync()
+            ms = 1000.0 * (time.perf_counter() - ts)
+            steps += 1
+            finished = []
+            for sid, v in self.resident.items():
+                v[1] -= 1
+                v[3].append(ms)
+                lat.append(ms)
+                pstep += v[0].n
+                if v[1] == 0:
+                    finished.append(sid)
+            for sid in finished:
+                req, _, adm, sm = self.resident.pop(sid)
+                pos, vel, dens = self.batch.download(sid)
+                self.batch.remove(sid)
+                done[req.rid] = Done(req.rid, pos, vel, dens, adm,
+                                     time.perf_counter() - t0 + offset, sm)
+            if on_step:
+                on_step(steps, ms, len(self.resident))
+        wall = time.perf_counter() - t0
+        lat = np.asarray(lat) if lat else np.zeros(1)
+        stats = dict(
+            requests=len(done), batched_steps=steps, particle_steps=int(pstep),
+            wall_s=wall, particle_steps_per_s=pstep / max(wall, 1e-9),
+            p50_step_ms=float(np.percentile(lat, 50)),
+            p99_step_ms=float(np.percentile(lat, 99)),
+            peak_resident_particles=int(peak_resident),
+            capacity_particles=int(self.capacity),
+        )
+        return done, stats
+
+
+def run_alone(req: Request, stream=None, tuning=None):
+    """The same request on its own single-scene handle (the comparison path
+    and the serial baseline)."""
+    sim = FluidSimulation(req.params, stream=stream)
+    sim.InitializeData(req.n, req.pos, req.vel)
+    if tuning:
+        sim.set_tuning(**tuning)
+    for _ in range(req.steps):
+        sim.step_async(req.dt, req.substeps)
+    out = sim.download()
+    sim.close()
+    return out

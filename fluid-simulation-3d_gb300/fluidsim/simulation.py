@@ -391,6 +391,9 @@ class Batch:
     def step(self, substeps: int):
         self._check(self._lib.sph_batch_step(self._h, int(substeps), self._stream))
 
+    def sync(self):
+        self._check(self._lib.sph_batch_sync(self._h, self._stream))
+
     def download(self, sid: int):
         n = self.sizes[int(sid)]
         pos = np.empty((n, 3), np.float32)

@@ -220,6 +220,10 @@ int sph_batch_add(sph_batch *b, const sph_params *params, uint32_t n,
 /* Remove a scene (its slot and particles are released at the next step). */
 int sph_batch_remove(sph_batch *b, uint32_t scene_id);
 
+/* Wait until the work queued on `stream` (and the batch's own stream) has
+ * finished. */
+int sph_batch_sync(sph_batch *b, void *stream);
+
 /* Advance every resident scene by one step of `substeps` substeps of its own
  * dt / substeps. */
 int sph_batch_step(sph_batch *b, int substeps, void *stream);
@@ -238,6 +242,10 @@ int sph_batch_get_tuning(const sph_batch *b, sph_tuning *t);
  * and report it in *best (may be NULL) and its ms per step in *best_ms. */
 int sph_batch_autotune(sph_batch *b, int substeps, int steps_per_trial,
                        sph_tuning *best, float *best_ms, void *stream);
+
+/* Device bytes an engine allocates per particle of capacity (state, sort,
+ * cell tables, neighbour lists): admission by an HBM budget divides by it. */
+uint64_t sph_bytes_per_particle(void);
 
 uint32_t sph_batch_num_scenes(const sph_batch *b);
 uint64_t sph_batch_num_particles(const sph_batch *b);
