@@ -359,6 +359,7 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
   LaunchCtx c = ctx_;
   c.block_nbr = tuning_.block;
   c.cell_tile = tuning_.cell_tile;
+  c.gather = tuning_.gather;
   c.max_blocks = 0;
   c.src_limit = static_cast<uint32_t>(capacity_);
   int cur = cur_;
@@ -658,37 +659,49 @@ int Engine::SetTuning(const sph_tuning& t) {
   if (t.cell_tile != 1 && t.cell_tile != 64 && t.cell_tile != 128 &&
       t.cell_tile != 192 && t.cell_tile != 256)
     return Fail(SPH_ERR_INVALID, "cell_tile must be 1, 64, 128, 192 or 256");
+  if (t.gather != 2 && t.gather != 4 && t.gather != 8)
+    return Fail(SPH_ERR_INVALID, "gather must be 2, 4 or 8");
   if (t.block != tuning_.block || t.particles_per_warp != tuning_.particles_per_warp ||
-      t.cell_tile != tuning_.cell_tile)
+      t.cell_tile != tuning_.cell_tile || t.gather != tuning_.gather)
     ReleaseGraphs();
   tuning_ = t;
   return SPH_OK;
 }
 
+// Coordinate search: block size x cell tile at the current gather batch,
+// then the gather batch at the best of those.
 int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
                      float* best_ms, cudaStream_t st) {
   if (steps_per_trial < 1) return Fail(SPH_ERR_INVALID, "steps_per_trial >= 1");
-  std::vector<sph_tuning> space;
-  for (int b : {64, 128, 256, 512})
-    for (int tile : {1, 64, 128, 256}) space.push_back(sph_tuning{b, tile, 32});
   sph_tuning win = tuning_;
   float win_ms = std::numeric_limits<float>::infinity();
   cudaEvent_t e0, e1;
   SPH_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
   SPH_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
   int rc = SPH_OK;
-  for (const sph_tuning& t : space) {
-    if ((rc = SetTuning(t)) != SPH_OK) break;
-    if ((rc = Step(substeps, st)) != SPH_OK) break;  // warm-up + capture
-    cudaEventRecord(e0, st);
-    for (int k = 0; k < steps_per_trial && rc == SPH_OK; ++k) rc = Step(substeps, st);
-    cudaEventRecord(e1, st);
-    if (rc != SPH_OK) break;
-    cudaEventSynchronize(e1);
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    ms /= static_cast<float>(steps_per_trial);
-    if (ms < win_ms) { win_ms = ms; win = t; }
+  for (int round = 0; round < 2 && rc == SPH_OK; ++round) {
+    std::vector<sph_tuning> space;
+    if (round == 0) {
+      for (int b : {64, 128, 256, 512})
+        for (int tile : {1, 64, 128, 256})
+          space.push_back(sph_tuning{b, tile, 32, tuning_.gather});
+    } else {
+      for (int g : {2, 4, 8})
+        space.push_back(sph_tuning{win.block, win.cell_tile, 32, g});
+    }
+    for (const sph_tuning& t : space) {
+      if ((rc = SetTuning(t)) != SPH_OK) break;
+      if ((rc = Step(substeps, st)) != SPH_OK) break;  // warm-up + capture
+      cudaEventRecord(e0, st);
+      for (int k = 0; k < steps_per_trial && rc == SPH_OK; ++k) rc = Step(substeps, st);
+      cudaEventRecord(e1, st);
+      if (rc != SPH_OK) break;
+      cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= static_cast<float>(steps_per_trial);
+      if (ms < win_ms) { win_ms = ms; win = t; }
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -136,7 +136,7 @@ __global__ void k_predict_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev& S = scenes[tile_scene(tile)];
+    const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
     const uint32_t s = tile.y + lane;
     const bool live = lane < tile_len(tile);
     uint32_t key = 0, hash = 0, id = 0;
@@ -270,7 +270,7 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev& S = scenes[tile_scene(tile)];
+    const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
     const uint32_t slot = tile.y + lane;
     if (lane >= tile_len(tile)) continue;
     const uint2 me = tmp_hi[slot];
@@ -318,7 +318,7 @@ __global__ void k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev& S = scenes[tile_scene(tile)];
+    const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
     const uint32_t i = tile.y + lane;
     const bool live = lane < tile_len(tile);
     const bool leader = live && cell_first[i] == i;
@@ -328,8 +328,7 @@ __global__ void k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
       const uint32_t c = q / 27u, o = q - c * 27u;
       const int L = __fns(lmask, 0, static_cast<int>(c) + 1);
       const uint32_t slot = tile.y + static_cast<uint32_t>(L);
-      const uint32_t hc = __ldg(hash_s + slot);
-      const uint32_t hh = hc + c_delta[o];
+      const uint32_t hh = __ldg(hash_s + slot) + c_delta[o];
       const uint32_t key = S.base + fastmod(hh, S.fm, S.n);
       const uint32_t b0 = __ldg(start + key), b1 = __ldg(start + key + 1);
       const float hf = __uint2float_rn(hh);
@@ -456,7 +455,7 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
   const uint32_t lt_mask = (1u << lane) - 1u;
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev& S = scenes[tile_scene(tile)];
+    const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
     const uint32_t i = tile.y + lane;
     const bool live = lane < tile_len(tile);
     const float4 me = live ? pred[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -598,7 +597,7 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev& S = scenes[tile_scene(tile)];
+    const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
     if (lane >= tile_len(tile)) continue;
     const uint32_t i = tile.y + lane;
     const float4 pi = pred[i];
@@ -674,7 +673,7 @@ __global__ void k_visc_integrate(
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
-    const SceneDev& S = scenes[tile_scene(tile)];
+    const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
     const bool live = lane < tile_len(tile);
     const uint32_t i = tile.y + lane;
     bool bad = false;

@@ -66,6 +66,8 @@ typedef struct sph_tuning {
                          per pass of the density kernel: 64, 128, 192 or
                          256 (default 128)                                */
   int32_t particles_per_warp; /* particles per warp: 32 (one per lane)    */
+  int32_t gather;     /* neighbour-list entries whose gathers the force
+                         kernels issue together: 2, 4 or 8 (default 4)    */
 } sph_tuning;
 
 /* Reference defaults of physicsWorld.h:96-106,145 and physicsWorld.cc:47,87. */

@@ -81,7 +81,7 @@ def lib():
             ctypes.c_double, ctypes.c_int, ctypes.POINTER(DebugF64)]
         L.sph_oracle_subset_f64.argtypes = [
             ctypes.POINTER(OracleParams), ctypes.c_uint32, _P, ctypes.c_uint32,
-            _P, ctypes.c_int, _P, _P]
+            _P, ctypes.c_int, _P, _P, _P, _P, _P]
         L.sph_oracle_hw_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -155,19 +155,24 @@ def substep_f64(params, pos, vel, dt, nthreads=0):
     return pos, vel, d
 
 
-def subset_f64(params, pred, subset, nthreads=0):
+def subset_f64(params, pred, subset, nthreads=0, with_abs=False):
     pred = np.ascontiguousarray(pred, dtype=np.float32)
     subset = np.ascontiguousarray(subset, dtype=np.uint32)
     m = subset.shape[0]
     dens = np.empty((m, 2))
     acc = np.empty((m, 3))
+    absp = np.empty(m)
+    sens = np.empty(m)
+    dsens = np.empty(m)
     prm = make_params(params)
     rc = lib().sph_oracle_subset_f64(ctypes.byref(prm), pred.shape[0],
                                      pred.ctypes.data, m, subset.ctypes.data,
-                                     nthreads, dens.ctypes.data, acc.ctypes.data)
+                                     nthreads, dens.ctypes.data, acc.ctypes.data,
+                                     absp.ctypes.data, sens.ctypes.data,
+                                     dsens.ctypes.data)
     if rc != 0:
         raise ValueError(f"oracle subset failed: {rc}")
-    return dens, acc
+    return (dens, acc, absp, sens, dsens) if with_abs else (dens, acc)
 
 
 def hw_threads() -> int:

@@ -402,7 +402,8 @@ int sph_oracle_substep_f64(const oracle_params* p, uint32_t n, double* pos,
 
 int sph_oracle_subset_f64(const oracle_params* p, uint32_t n, const float* pred,
                           uint32_t m, const uint32_t* subset, int nthreads,
-                          double* out_dens, double* out_acc) {
+                          double* out_dens, double* out_acc, double* out_abs,
+                          double* out_sens, double* out_dsens) {
   if (!ParamsOk(p, n) || !pred || (m && !subset)) return -1;
   for (uint32_t t = 0; t < m; ++t)
     if (subset[t] >= n) return -2;
@@ -433,7 +434,7 @@ int sph_oracle_subset_f64(const oracle_params* p, uint32_t n, const float* pred,
     const double density = dens[2 * i], nearDensity = dens[2 * i + 1];
     const double pressure = (density - S.rho0) * S.k;
     const double nearPressure = nearDensity * S.kn;
-    double fx = 0, fy = 0, fz = 0;
+    double fx = 0, fy = 0, fz = 0, absSum = 0, sens = 0, dsens = 0;
     ForNeighbours(L, n, S.r, q0, [&](uint32_t j) {
       if (j == i) return;
       const double* q = &pd[3 * j];
@@ -448,7 +449,20 @@ int sph_oracle_subset_f64(const oracle_params* p, uint32_t n, const float* pred,
       double a = K.dpow2(dist) * sp / dens[2 * j];
       double b = K.dpow3(dist) * snp / dens[2 * j + 1];
       fx += dx * (a + b); fy += dy * (a + b); fz += dz * (a + b);
+      absSum += std::fabs(a) + std::fabs(b);
+      // d(term)/d(log rho) for rho_i and rho_j: what an FP32 rounding of
+      // the densities moves the term by, (rho - rho0) * k cancelling
+      sens += std::fabs(K.dpow2(dist)) * 0.5 * S.k *
+              (dens[2 * i] + dens[2 * j]) / dens[2 * j];
+      // d(term)/d(dist): what a rounding of the positions moves the term by
+      // (a pair at the edge of the support has a term linear in r - dist)
+      if (dist <= S.r)
+        dsens += K.dscale2 * std::fabs(sp / dens[2 * j]) +
+                 2.0 * (S.r - dist) * K.dscale3 * std::fabs(snp / dens[2 * j + 1]);
     });
+    if (out_abs) out_abs[t] = absSum / std::fabs(density);
+    if (out_sens) out_sens[t] = sens / std::fabs(density);
+    if (out_dsens) out_dsens[t] = dsens / std::fabs(density);
     if (out_dens) { out_dens[2 * t] = density; out_dens[2 * t + 1] = nearDensity; }
     if (out_acc) {
       out_acc[3 * t] = fx / density;

@@ -87,10 +87,19 @@ int sph_oracle_substep_f64(const oracle_params *p, uint32_t n, double *pos,
  * given: densities of every particle are recomputed in FP64 from the FP32
  * predicted positions (the physics does not depend on the grid), then the
  * pressure acceleration (pressureForce/density, physicsWorld.cc:367-421) is
- * evaluated for the `m` listed particles. out_dens [2m], out_acc [3m]. */
+ * evaluated for the `m` listed particles. out_dens [2m], out_acc [3m],
+ * out_abs [m] = sum over neighbours of |pressure term| / density (the scale
+ * of the cancelling sum), out_sens [m] = sum over neighbours of the terms'
+ * sensitivity to a relative change of the densities (pressure (rho-rho0)*k
+ * cancels near rho0, so FP32 rounding of rho moves the terms by about
+ * out_sens * 2^-24), out_dsens [m] = sum over neighbours of
+ * |d term / d dist| / density (a pair at the edge of the support has a term
+ * linear in r - dist, so a rounding of the positions by e moves the
+ * acceleration by up to out_dsens * e); any output may be NULL. */
 int sph_oracle_subset_f64(const oracle_params *p, uint32_t n, const float *pred,
                           uint32_t m, const uint32_t *subset, int nthreads,
-                          double *out_dens, double *out_acc);
+                          double *out_dens, double *out_acc, double *out_abs,
+                          double *out_sens, double *out_dsens);
 
 /* Number of hardware threads the oracle would use for nthreads <= 0. */
 int sph_oracle_hw_threads(void);
