@@ -2,15 +2,30 @@
 //
 // Layout in HBM (one engine, S scenes concatenated, capacity P particles):
 //   pos[P], vel[P]      float4 state in the current sorted layout; pos.w holds
-//                       the particle's global id as raw bits
-//   pred[P]             float4 (predicted position, float(cell hash))
+//                       the particle's index in its scene as raw bits
+//   pred[P]             float4 (predicted position, cell index as raw bits)
 //   dens_a[P]           float2 (density, near density)
 //   dens_b[P]           float4 (1/rho, P/rho, 1/rho_n, Pn/rho_n)
 //   velp[P]             float4 post-pressure velocity (Jacobi snapshot)
-//   keyrank[P]          uint2 (global key, arrival rank in the key bucket)
-//   tmp[P]              uint2 (id, source slot) bucketed, pre-canonical
+//   keyrank[P]          uint4 (global key, arrival rank in the key bucket,
+//                       cell index, particle index)
+//   tmp_hi[P], tmp_src[P] bucketed (cell index, particle index) and source
+//                       slot, before the order inside each bucket is fixed
 //   count[P], start[P+1] uint32 counting-sort table; a scene owns keys
 //                       [base, base+n) so start[] is also its slot range
+//   cell_tab[27P]       per cell (at its first slot) its neighbour runs as 9
+//                       rows (dy, dz) of 3 runs (dx = -1, 0, +1)
+//
+// The layout is sorted by an internal cell index, not by the reference's
+// HashCell key: the index is linear in the cell coordinates with x fastest
+// over a grid anchored at the box, so the three x-neighbour cells of a row
+// are consecutive keys and, when their buckets hold only those cells, one
+// contiguous run of slots. Consecutive slots are then spatial neighbours,
+// which the neighbour walks and the force gathers turn into cache hits. The
+// set of pairs within the cutoff does not depend on the key function (every
+// such pair lies in adjacent cells, and a run holds only its own cell), so
+// the physics is the reference's; the reference's own key order
+// (spatialLookup / startIndices) is rebuilt on demand by the debug pass.
 #pragma once
 
 #include <cstdint>
@@ -28,9 +43,11 @@ constexpr int kTile = 32;
 
 // Per-scene descriptor, built on the host from sph_params.
 struct SceneDev {
-  uint32_t n;         // particles (and key-table size: key = hash % n)
+  uint32_t n;         // particles (and key-table size: key = index % n)
   uint32_t base;      // first slot of the scene's current layout / table
   uint64_t fm;        // Lemire magic for x % n
+  uint32_t gx0, gy0, gz0;  // origin cell of the internal grid (int32 bits)
+  uint32_t gwy, gwz;  // y and z strides of the internal cell index
   float r;            // interaction radius
   float cut_lt;       // d2 <= cut_lt  <=>  d2 <= sqrRadius && sqrtf(d2) < r
   float cut_le;       // d2 <= cut_le  <=>  d2 <= sqrRadius && sqrtf(d2) <= r
@@ -86,13 +103,20 @@ __device__ __forceinline__ uint32_t hash_of(const SceneDev& S, float3 pr) {
   return hash_cell(cell_of(pr.x, S.r), cell_of(pr.y, S.r), cell_of(pr.z, S.r));
 }
 
-// Hash delta of the neighbour offset o in the reference's table order
-// (physicsWorld.h:131-143: dx outermost, dz innermost):
-// hash(c + d) = hash(c) + dx*kHashX + dy*kHashY + dz*kHashZ (mod 2^32).
-__device__ __forceinline__ uint32_t offset_delta(int o) {
-  const int dx = o / 9 - 1, dy = (o / 3) % 3 - 1, dz = o % 3 - 1;
-  return static_cast<uint32_t>(dx) * kHashX + static_cast<uint32_t>(dy) * kHashY +
-         static_cast<uint32_t>(dz) * kHashZ;
+// Internal cell index of the sort (the reference's cells, another key):
+// (cx - x0) + (cy - y0) * wy + (cz - z0) * wz modulo 2^32. Linear in the
+// wrapped cell coordinates like HashCell, so index(c + d) = index(c) + dx +
+// dy*wy + dz*wz for every cell, and distinct neighbour offsets never share
+// an index (|dx + dy*wy + dz*wz| < 2^32).
+__device__ __forceinline__ uint32_t cell_index(const SceneDev& S, float3 pr) {
+  const uint32_t cx = static_cast<uint32_t>(cell_of(pr.x, S.r)) - S.gx0;
+  const uint32_t cy = static_cast<uint32_t>(cell_of(pr.y, S.r)) - S.gy0;
+  const uint32_t cz = static_cast<uint32_t>(cell_of(pr.z, S.r)) - S.gz0;
+  return cx + cy * S.gwy + cz * S.gwz;
 }
+
+// Run-length flag of a cell-table row whose three x-runs are one contiguous
+// run (stored in the row's first entry; the other two entries are empty).
+constexpr uint32_t kRunMerged = 0x80000000u;
 
 }  // namespace sph

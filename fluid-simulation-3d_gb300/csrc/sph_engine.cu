@@ -26,6 +26,26 @@ template <class Pred> float LargestWith(float r, Pred ok) {
   return x;
 }
 
+// Internal cell grid along one axis: the cells of [-h, h] (the box) plus a
+// margin of 2 cells each side; returns the cell count, origin = first cell.
+// Any origin and size give the same physics (they shape the layout only),
+// but the count is kept in [5, 2^15] so that the y and z strides stay below
+// 2^30 and the 27 offsets dx + dy*wy + dz*wz of a cell are distinct modulo
+// 2^32; a larger box wraps onto the grid: cells that are not neighbours may
+// then share an index and a run, and the cutoff test drops their pairs, as
+// the reference's does for the cells its HashCell collides.
+uint32_t GridAxis(float h, float r, uint32_t* origin) {
+  const double a = std::floor(static_cast<double>(-h) / r);
+  const double b = std::floor(static_cast<double>(h) / r);
+  double lo = std::min(a, b) - 2.0, hi = std::max(a, b) + 2.0;
+  if (!std::isfinite(lo) || !std::isfinite(hi) || lo < -1e9 || hi > 1e9) {
+    lo = 0.0;
+    hi = 1023.0;
+  }
+  *origin = static_cast<uint32_t>(static_cast<int32_t>(lo));
+  return static_cast<uint32_t>(std::min(hi - lo + 1.0, 32768.0));
+}
+
 SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base,
                       float sub_dt) {
   SceneDev d{};
@@ -34,6 +54,11 @@ SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base,
   d.fm = (~static_cast<uint64_t>(0)) / n + 1;
   const float r = p.radius;
   d.r = r;
+  const uint32_t gx = GridAxis(p.bound[0] * 0.5f, r, &d.gx0);
+  const uint32_t gy = GridAxis(p.bound[1] * 0.5f, r, &d.gy0);
+  GridAxis(p.bound[2] * 0.5f, r, &d.gz0);
+  d.gwy = gx;
+  d.gwz = gx * gy;  // modulo 2^32
   const float t_lt = LargestWith(r, [r](float s) { return s < r; });
   const float t_le = LargestWith(r, [r](float s) { return s <= r; });
   d.cut_lt = std::min(p.cutoff_sq, t_lt);
@@ -87,7 +112,8 @@ Engine::~Engine() {
                   ctx_.count, ctx_.start,
                   ctx_.partial, d_out4_, d_status_, d_dbg_hash_, d_dbg_key_,
                   d_dbg_accp_, d_dbg_velv_, d_dbg_velp_, d_dbg_start_,
-                  d_dbg_scratch_};
+                  d_dbg_count_, d_dbg_partial_, d_dbg_keyrank_, d_dbg_tmp_,
+                  d_dbg_sorted_, d_dbg_scratch_};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -374,7 +400,6 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
     c.pos2 = d_pos_[1 - cur];
     c.vel2 = d_vel_[1 - cur];
     const bool dbg = debug_ && ss == 0;
-    c.dbg_key = dbg ? d_dbg_key_ : nullptr;
     c.dbg_accp = dbg ? d_dbg_accp_ : nullptr;
     c.dbg_velv = dbg ? d_dbg_velv_ : nullptr;
     const Tiles& first = ss == 0 ? told : tnew;
@@ -393,13 +418,7 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
     if (e == cudaSuccess) e = launch_scan(c, total_, st);
     if (e == cudaSuccess) e = launch_sort_reorder(c, first, tnew, total_, st);
     mark(2);
-    if (e == cudaSuccess && dbg) {
-      e = cudaMemcpyAsync(d_dbg_start_, c.start, sizeof(uint32_t) * (total_ + 1),
-                          cudaMemcpyDeviceToDevice, st);
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_dbg_hash_, c.hash_s, sizeof(uint32_t) * total_,
-                            cudaMemcpyDeviceToDevice, st);
-    }
+    if (e == cudaSuccess && dbg) e = launch_ref_lookup(c, tnew, total_, st);
     if (e == cudaSuccess) e = launch_density(c, tnew, st);
     mark(3);
     if (e == cudaSuccess) e = launch_pressure(c, tnew, st);
@@ -569,9 +588,23 @@ int Engine::DebugEnable(bool on) {
     chk(Alloc(&d_dbg_velv_, C));
     chk(Alloc(&d_dbg_velp_, C));
     chk(Alloc(&d_dbg_start_, C + 1));
-    // hash 4 + key 4 + three float3 (36) per particle
-    chk(cudaMalloc(&d_dbg_scratch_, C * 44 + 64));
+    chk(Alloc(&d_dbg_count_, C));
+    chk(Alloc(&d_dbg_partial_, scan_partials_needed(C)));
+    chk(Alloc(&d_dbg_keyrank_, C));
+    chk(Alloc(&d_dbg_tmp_, C));
+    chk(Alloc(&d_dbg_sorted_, C));
+    // three float3 (36) per particle
+    chk(cudaMalloc(&d_dbg_scratch_, C * 36 + 64));
+    if (e == cudaSuccess) e = cudaMemset(d_dbg_count_, 0, C * sizeof(uint32_t));
     if (e != cudaSuccess) return CudaFail(e, "debug buffers");
+    ctx_.dbg_hash = d_dbg_hash_;
+    ctx_.dbg_key = d_dbg_key_;
+    ctx_.dbg_count = d_dbg_count_;
+    ctx_.dbg_start = d_dbg_start_;
+    ctx_.dbg_partial = d_dbg_partial_;
+    ctx_.dbg_keyrank = d_dbg_keyrank_;
+    ctx_.dbg_tmp = d_dbg_tmp_;
+    ctx_.dbg_sorted = d_dbg_sorted_;
   }
   if (debug_ != on) ReleaseGraphs();
   debug_ = on;
@@ -588,21 +621,20 @@ int Engine::DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
   if (!debug_valid_) return Fail(SPH_ERR_STATE, "no captured substep");
   const uint32_t n = scenes_[id].n;
   const uint32_t b = old_base_[id];
-  uint8_t* s = static_cast<uint8_t*>(d_dbg_scratch_);
-  uint32_t* sh = reinterpret_cast<uint32_t*>(s);
-  uint32_t* sk = sh + n;
-  float* sa = reinterpret_cast<float*>(sk + n);
+  float* sa = static_cast<float*>(d_dbg_scratch_);
   float* sp = sa + 3 * static_cast<uint64_t>(n);
   float* sv = sp + 3 * static_cast<uint64_t>(n);
-  SPH_CUDA(launch_export_debug(b, n, d_pos_[cur_], d_dbg_hash_, d_dbg_key_,
-                               d_dbg_accp_, d_dbg_velp_, d_dbg_velv_, sh, sk,
-                               sa, sp, sv, st), "debug export kernel");
+  SPH_CUDA(launch_export_debug(b, n, d_pos_[cur_], d_dbg_accp_, d_dbg_velp_,
+                               d_dbg_velv_, sa, sp, sv, st), "debug export kernel");
   auto d2h = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
     if (!dst) return cudaSuccess;
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
   };
-  SPH_CUDA(d2h(hash, sh, 4ull * n), "download");
-  SPH_CUDA(d2h(key, sk, 4ull * n), "download");
+  // The reference lookup (launch_ref_lookup) is indexed by particle (hash,
+  // key) and by lookup slot (sorted ids, start) within the scene's range.
+  SPH_CUDA(d2h(hash, d_dbg_hash_ + b, 4ull * n), "download");
+  SPH_CUDA(d2h(key, d_dbg_key_ + b, 4ull * n), "download");
+  SPH_CUDA(d2h(sorted_ids, d_dbg_sorted_ + b, 4ull * n), "download");
   SPH_CUDA(d2h(accp, sa, 12ull * n), "download");
   SPH_CUDA(d2h(velp, sp, 12ull * n), "download");
   SPH_CUDA(d2h(velv, sv, 12ull * n), "download");
@@ -610,23 +642,6 @@ int Engine::DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
   SPH_CUDA(cudaMemcpyAsync(st_raw.data(), d_dbg_start_ + b, 4ull * (n + 1),
                            cudaMemcpyDeviceToHost, st), "download start");
   SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-  if (sorted_ids) {
-    // ids of the captured layout in slot order (pos.w raw bits), ordered by
-    // (hash, index) inside each key bucket; the reference's lookup order is
-    // (key, index): sort each bucket by index.
-    std::vector<float4> p(n);
-    SPH_CUDA(cudaMemcpy(p.data(), d_pos_[cur_] + b, sizeof(float4) * n,
-                        cudaMemcpyDeviceToHost), "download ids");
-    for (uint32_t k = 0; k < n; ++k) {
-      uint32_t bits;
-      std::memcpy(&bits, &p[k].w, 4);
-      sorted_ids[k] = bits;
-    }
-    for (uint32_t k = 0; k < n; ++k) {
-      const uint32_t s0 = st_raw[k] - b, s1 = st_raw[k + 1] - b;
-      if (s1 > s0 + 1 && s1 <= n) std::sort(sorted_ids + s0, sorted_ids + s1);
-    }
-  }
   if (start) {
     for (uint32_t k = 0; k < n; ++k)
       start[k] = st_raw[k + 1] > st_raw[k] ? st_raw[k] - b : 0x7fffffffu;

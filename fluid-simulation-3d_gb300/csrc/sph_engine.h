@@ -111,6 +111,11 @@ class Engine {
   float4* d_dbg_velv_ = nullptr;
   float4* d_dbg_velp_ = nullptr;
   uint32_t* d_dbg_start_ = nullptr;
+  uint32_t* d_dbg_count_ = nullptr;
+  uint32_t* d_dbg_partial_ = nullptr;
+  uint2* d_dbg_keyrank_ = nullptr;
+  uint32_t* d_dbg_tmp_ = nullptr;
+  uint32_t* d_dbg_sorted_ = nullptr;
   void* d_dbg_scratch_ = nullptr;
 
   // Neighbour-list capacity per particle (pairs with dist <= r); a particle

@@ -1,25 +1,29 @@
 // SPH substep kernels for GB300 (sm_103a).
 //
 // One substep (engine/physics/physicsWorld.cc:39-111) is:
-//   k_predict_hash   gravity + prediction + cell hash + key, counting-sort
+//   k_predict_hash   gravity + prediction + cell index + key, counting-sort
 //                    histogram (warp-aggregated atomics)    :42-48, :473-482
 //   k_scan_*         exclusive prefix of the key histogram = start table
 //   k_scatter        bucket each particle at start[key] + arrival rank
 //   k_reorder        deterministic order inside each bucket and gather of
 //                    the state into SoA float4                :484-496
-//   k_cell_table     per cell, its 27 neighbour runs (the bucket walk of
+//   k_cell_table     per cell, its neighbour runs (the bucket walk of
 //                    :331-346 resolved once per cell instead of per particle)
 //   k_density        density / near density and neighbour lists :304-365
 //   k_pressure       pressure + near pressure over the list   :367-422
 //   k_visc_integrate Jacobi viscosity over the list, integrate, box
 //                    collision, next substep's prediction    :424-464, :81-108
+// and, when a substep is captured for export, k_ref_* rebuild the
+// reference's own spatial lookup (HashCell keys, (key, index) order and
+// startIndices, :466-496) from the same predicted positions.
 //
-// Inside a key bucket particles are ordered by (cell hash, index), so every
-// cell is a contiguous run of slots (the reference orders a bucket only by
-// key; its canonical (key, index) order is rebuilt from this one on export).
-// Every kernel is a persistent, segmented launch: warps stride over a tile
-// table of (scene, first slot) runs of up to 32 particles of one scene, so one
-// launch serves any number of scenes of uneven sizes.
+// The sort key is the internal cell index (sph_device.cuh) modulo the scene
+// size; inside a key bucket particles are ordered by (cell index, particle
+// index), so every cell is a contiguous run of slots and the three cells of
+// an x-row usually one run. Every kernel is a persistent, segmented launch:
+// warps stride over a tile table of (scene, first slot) runs of up to 32
+// particles of one scene, so one launch serves any number of scenes of
+// uneven sizes.
 #include "sph_kernels.h"
 
 namespace sph {
@@ -27,21 +31,6 @@ namespace sph {
 namespace {
 
 constexpr uint32_t kFull = 0xffffffffu;
-
-constexpr uint32_t Delta(int o) {
-  return static_cast<uint32_t>(o / 9 - 1) * kHashX +
-         static_cast<uint32_t>((o / 3) % 3 - 1) * kHashY +
-         static_cast<uint32_t>(o % 3 - 1) * kHashZ;
-}
-
-// hash(c + offset_o) - hash(c) for the 27 offsets of physicsWorld.h:131-143.
-// HashCell is linear modulo 2^32, so the neighbour buckets of a cell depend
-// only on its hash.
-__constant__ uint32_t c_delta[27] = {
-    Delta(0),  Delta(1),  Delta(2),  Delta(3),  Delta(4),  Delta(5),  Delta(6),
-    Delta(7),  Delta(8),  Delta(9),  Delta(10), Delta(11), Delta(12), Delta(13),
-    Delta(14), Delta(15), Delta(16), Delta(17), Delta(18), Delta(19), Delta(20),
-    Delta(21), Delta(22), Delta(23), Delta(24), Delta(25), Delta(26)};
 
 __device__ __forceinline__ uint32_t warp_id_global() {
   return blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -100,9 +89,10 @@ __device__ __forceinline__ uint32_t aggregated_rank(uint32_t* count,
   return base + __popc(peers & ((1u << lane) - 1u));
 }
 
-// Neighbour walk of a particle through its cell's 27 runs (table built by
-// k_cell_table): every candidate the reference's bucket loops would accept,
-// in the reference's offset order.
+// Neighbour walk of a particle through its cell's table (k_cell_table): the
+// particles of the 27 neighbour cells -- every candidate the reference's
+// bucket loops would accept within the cutoff -- row by row, a merged row as
+// one run.
 template <class F>
 __device__ __forceinline__ void walk_runs(const uint2* __restrict__ cell_tab,
                                           uint32_t cf,
@@ -110,21 +100,31 @@ __device__ __forceinline__ void walk_runs(const uint2* __restrict__ cell_tab,
                                           F&& visit) {
   const uint2* row = cell_tab + static_cast<uint64_t>(cf) * 27u;
 #pragma unroll 1
-  for (int o = 0; o < 27; ++o) {
-    const uint2 run = __ldg(row + o);
+  for (int w = 0; w < 9; ++w, row += 3) {
+    const uint2 m = __ldg(row);
+    if (m.y & kRunMerged) {
+      const uint32_t e = m.x + (m.y & ~kRunMerged);
 #pragma unroll 1
-    for (uint32_t j = run.x; j < run.x + run.y; ++j) visit(j, __ldg(pred + j));
+      for (uint32_t j = m.x; j < e; ++j) visit(j, __ldg(pred + j));
+    } else {
+#pragma unroll 1
+      for (int k = 0; k < 3; ++k) {
+        const uint2 run = k ? __ldg(row + k) : m;
+#pragma unroll 1
+        for (uint32_t j = run.x; j < run.x + run.y; ++j) visit(j, __ldg(pred + j));
+      }
+    }
   }
 }
 
 // ----------------------------------------------------------------- predict
 __device__ __forceinline__ void predict_key(const SceneDev& S, float4 p,
                                             float4 v, uint32_t& key,
-                                            uint32_t& hash) {
+                                            uint32_t& cell) {
   float3 vn, pr;
   predict(S, p, v, vn, pr);
-  hash = hash_of(S, pr);
-  key = S.base + fastmod(hash, S.fm, S.n);
+  cell = cell_index(S, pr);
+  key = S.base + fastmod(cell, S.fm, S.n);
 }
 
 __global__ void k_predict_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
@@ -139,14 +139,14 @@ __global__ void k_predict_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
     const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
     const uint32_t s = tile.y + lane;
     const bool live = lane < tile_len(tile);
-    uint32_t key = 0, hash = 0, id = 0;
+    uint32_t key = 0, cell = 0, id = 0;
     if (live) {
       const float4 p = pos[s];
-      predict_key(S, p, vel[s], key, hash);
+      predict_key(S, p, vel[s], key, cell);
       id = __float_as_uint(p.w);
     }
     const uint32_t r = aggregated_rank(count, key, live);
-    if (live) keyrank[s] = make_uint4(key, r, hash, id);
+    if (live) keyrank[s] = make_uint4(key, r, cell, id);
   }
 }
 
@@ -250,9 +250,9 @@ __global__ void k_scatter(const uint2* __restrict__ tiles, uint32_t ntiles,
 
 // ----------------------------------------------------------------- reorder
 // Thread per bucketed slot: rank the particle inside its bucket by
-// (hash, index), recompute its gravity/prediction exactly as k_predict_hash
-// did, and write the state to its final slot, plus the first slot of its
-// cell (its run of equal hash).
+// (cell index, particle index), recompute its gravity/prediction exactly as
+// k_predict_hash did, and write the state to its final slot, plus the first
+// slot of its cell (its run of equal cell index).
 __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
                           const SceneDev* __restrict__ scenes,
                           const uint2* __restrict__ tmp_hi,
@@ -265,8 +265,7 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
                           float4* __restrict__ pred,
                           uint32_t* __restrict__ hash_s,
                           uint32_t* __restrict__ cell_first,
-                          uint32_t* __restrict__ dbg_key, uint32_t src_limit,
-                          uint32_t* status) {
+                          uint32_t src_limit, uint32_t* status) {
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -280,10 +279,10 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
     const float4 v = vel_in[src];
     float3 vn, pr;
     predict(S, p, v, vn, pr);
-    const uint32_t hash = hash_of(S, pr);
-    const uint32_t key = S.base + fastmod(hash, S.fm, S.n);
+    const uint32_t cell = cell_index(S, pr);
+    const uint32_t key = S.base + fastmod(cell, S.fm, S.n);
     const uint32_t b0 = start[key], b1 = start[key + 1];
-    if (slot < b0 || slot >= b1 || hash != me.x) {
+    if (slot < b0 || slot >= b1 || cell != me.x) {
       flag(status, kStatusRange);
       continue;
     }
@@ -296,19 +295,45 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
     const uint32_t f = b0 + rank;
     pos_out[f] = p;
     vel_out[f] = make_float4(vn.x, vn.y, vn.z, 0.0f);
-    pred[f] = make_float4(pr.x, pr.y, pr.z, __uint2float_rn(hash));
-    hash_s[f] = hash;
+    pred[f] = make_float4(pr.x, pr.y, pr.z, __uint_as_float(cell));
+    hash_s[f] = cell;
     cell_first[f] = b0 + below;
-    if (dbg_key) dbg_key[f] = key - S.base;
   }
 }
 
 // -------------------------------------------------------------- cell table
-// For each cell (its first slot), the 27 runs its particles visit: for
-// offset o the bucket of hash(c)+delta_o holds, sorted by hash, the entries
-// the reference keeps -- those whose float(hash) equals float(hash(c+o))
-// (:346) -- as one contiguous run. Lanes take (cell, offset) pairs of the
-// warp's tile in parallel.
+// The run of cell index `cell` in its key bucket. A bucket is sorted by cell
+// index, so the cell's particles are one run and entries of other cells
+// that share the bucket are left out, as the reference's float(hash) test
+// leaves them out (:346); a bucket holding a single cell is the common case
+// and is recognised from its first and last entries.
+__device__ __forceinline__ uint2 bucket_run(const SceneDev& S, uint32_t cell,
+                                            const uint32_t* __restrict__ hash_s,
+                                            const uint32_t* __restrict__ start) {
+  const uint32_t key = S.base + fastmod(cell, S.fm, S.n);
+  const uint32_t b0 = __ldg(start + key), b1 = __ldg(start + key + 1);
+  uint32_t first = b0, len = 0;
+  if (b1 > b0) {
+    const uint32_t h0 = __ldg(hash_s + b0), h1 = __ldg(hash_s + b1 - 1);
+    if (h0 == cell && h1 == cell) {
+      len = b1 - b0;
+    } else if (h0 <= cell && cell <= h1) {
+      for (uint32_t u = b0; u < b1; ++u) {
+        const bool eq = __ldg(hash_s + u) == cell;
+        if (eq && len == 0) first = u;
+        len += eq ? 1u : 0u;
+      }
+    }
+  }
+  return make_uint2(first, len);
+}
+
+// For each cell (its first slot), the runs of its 27 neighbour cells as 9
+// rows (dy, dz) of three x-runs. The x-neighbours of a row have consecutive
+// cell indices, hence consecutive keys; when their runs are adjacent in the
+// layout (their buckets hold no other cell -- the usual case inside the box)
+// the row is stored as one run flagged kRunMerged. Lanes take (cell, row)
+// pairs of the warp's tile in parallel.
 __global__ void k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
                              const SceneDev* __restrict__ scenes,
                              const uint32_t* __restrict__ hash_s,
@@ -323,34 +348,42 @@ __global__ void k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
     const bool live = lane < tile_len(tile);
     const bool leader = live && cell_first[i] == i;
     const uint32_t lmask = __ballot_sync(kFull, leader);
-    const uint32_t pairs = __popc(lmask) * 27u;
+    const uint32_t pairs = __popc(lmask) * 9u;
     for (uint32_t q = lane; q < pairs; q += 32) {
-      const uint32_t c = q / 27u, o = q - c * 27u;
+      const uint32_t c = q / 9u, w = q - c * 9u;
       const int L = __fns(lmask, 0, static_cast<int>(c) + 1);
       const uint32_t slot = tile.y + static_cast<uint32_t>(L);
-      const uint32_t hh = __ldg(hash_s + slot) + c_delta[o];
-      const uint32_t key = S.base + fastmod(hh, S.fm, S.n);
-      const uint32_t b0 = __ldg(start + key), b1 = __ldg(start + key + 1);
-      const float hf = __uint2float_rn(hh);
-      // The bucket is sorted by hash, so the entries with float(hash) == hf
-      // are one run; a bucket holding a single cell is the common case and
-      // is recognised from its first and last entries.
-      uint32_t first = b1, len = 0;
-      if (b1 > b0) {
-        const float f0 = __uint2float_rn(__ldg(hash_s + b0));
-        const float f1 = __uint2float_rn(__ldg(hash_s + b1 - 1));
-        if (f0 == hf && f1 == hf) {
-          first = b0;
-          len = b1 - b0;
-        } else if (f0 <= hf && hf <= f1) {
-          for (uint32_t u = b0; u < b1; ++u) {
-            const bool eq = __uint2float_rn(__ldg(hash_s + u)) == hf;
-            if (eq && len == 0) first = u;
-            len += eq ? 1u : 0u;
-          }
+      const uint32_t dy = w / 3u - 1u, dz = w % 3u - 1u;  // mod 2^32
+      const uint32_t mid = __ldg(hash_s + slot) + dy * S.gwy + dz * S.gwz;
+      uint2 run[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        run[k] = bucket_run(S, mid + static_cast<uint32_t>(k - 1), hash_s, start);
+      uint32_t f = 0, e = 0;
+      bool any = false, adjacent = true;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (run[k].y == 0) continue;
+        if (!any) {
+          f = run[k].x;
+          e = f + run[k].y;
+          any = true;
+        } else if (run[k].x == e) {
+          e += run[k].y;
+        } else {
+          adjacent = false;
         }
       }
-      cell_tab[static_cast<uint64_t>(slot) * 27u + o] = make_uint2(first, len);
+      uint2* out = cell_tab + static_cast<uint64_t>(slot) * 27u + 3u * w;
+      if (adjacent) {
+        out[0] = make_uint2(f, (e - f) | kRunMerged);
+        out[1] = make_uint2(e, 0u);
+        out[2] = make_uint2(e, 0u);
+      } else {
+        out[0] = run[0];
+        out[1] = run[1];
+        out[2] = run[2];
+      }
     }
   }
 }
@@ -472,6 +505,7 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
       const uint32_t cfc = __shfl_sync(kFull, cf, c0);
       uint2 run = make_uint2(0u, 0u);
       if (lane < 27) run = __ldg(cell_tab + static_cast<uint64_t>(cfc) * 27u + lane);
+      run.y &= ~kRunMerged;
       const uint32_t incl = warp_incl_scan(run.y);
       const uint32_t excl = incl - run.y;
       const uint32_t total = __shfl_sync(kFull, incl, 31);
@@ -643,7 +677,7 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
 // CalculateViscosityForce (:424-464) over the neighbour list reading the
 // post-pressure snapshot (Jacobi); poly6 = (r^2 - d^2)^3 for dist < r. Then
 // pos += v*dt and the box collision (:81-108). With fuse_next the next
-// substep's prediction / hash / histogram (k_predict_hash) runs here on the
+// substep's prediction / cell index / histogram (k_predict_hash) runs here on the
 // new state.
 __device__ __forceinline__ void visc_pair(const SceneDev& S, float3 p,
                                           float4 vi, float4 q, float4 vj,
@@ -677,7 +711,7 @@ __global__ void k_visc_integrate(
     const bool live = lane < tile_len(tile);
     const uint32_t i = tile.y + lane;
     bool bad = false;
-    uint32_t key = 0, hash = 0, id = 0;
+    uint32_t key = 0, cell = 0, id = 0;
     if (live) {
       const float4 pi = pred[i];
       const float3 p = make_float3(pi.x, pi.y, pi.z);
@@ -727,11 +761,11 @@ __global__ void k_visc_integrate(
         if (id < S.n) out4[S.base + id] = make_float4(x.x, x.y, x.z, 0.34f);
         else bad = true;
       }
-      if (fuse_next) predict_key(S, x, v4, key, hash);
+      if (fuse_next) predict_key(S, x, v4, key, cell);
     }
     if (fuse_next) {
       const uint32_t r = aggregated_rank(count, key, live);
-      if (live) keyrank[i] = make_uint4(key, r, hash, id);
+      if (live) keyrank[i] = make_uint4(key, r, cell, id);
     }
     if (__any_sync(kFull, bad) && lane == 0) flag(status, kStatusNonFinite);
   }
@@ -764,16 +798,91 @@ __global__ void k_export(uint32_t first, uint32_t n,
   }
 }
 
-// Debug intermediates of one scene to caller order.
+// ------------------------------------------------------ reference lookup
+// The reference's spatial lookup of a captured substep (UpdateSpatialLookup,
+// physicsWorld.cc:466-496) from the predicted positions of the sorted
+// layout, by a counting sort of its own: HashCell and key = hash % n of every
+// particle (written by particle index), entries in (key, particle index)
+// order, and the start of every key.
+__global__ void k_ref_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
+                           const SceneDev* __restrict__ scenes,
+                           const float4* __restrict__ pred,
+                           const float4* __restrict__ pos,
+                           uint32_t* __restrict__ count,
+                           uint2* __restrict__ keyrank,
+                           uint32_t* __restrict__ ohash,
+                           uint32_t* __restrict__ okey, uint32_t* status) {
+  const uint32_t lane = lane_id();
+  for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
+    const uint2 tile = tiles[t];
+    const SceneDev S = scenes[tile_scene(tile)];
+    const uint32_t s = tile.y + lane;
+    const bool live = lane < tile_len(tile);
+    uint32_t key = 0, hash = 0, id = 0;
+    if (live) {
+      const float4 q = pred[s];
+      hash = hash_of(S, make_float3(q.x, q.y, q.z));
+      key = S.base + fastmod(hash, S.fm, S.n);
+      id = __float_as_uint(pos[s].w);
+    }
+    const uint32_t r = aggregated_rank(count, key, live);
+    if (!live) continue;
+    keyrank[s] = make_uint2(key, r);
+    if (id < S.n) {
+      ohash[S.base + id] = hash;
+      okey[S.base + id] = key - S.base;
+    } else {
+      flag(status, kStatusRange);
+    }
+  }
+}
+
+// Bucket every particle index at start[key] + arrival rank.
+__global__ void k_ref_scatter(const uint2* __restrict__ tiles, uint32_t ntiles,
+                              const float4* __restrict__ pos,
+                              const uint2* __restrict__ keyrank,
+                              const uint32_t* __restrict__ start,
+                              uint32_t total, uint32_t* __restrict__ tmp,
+                              uint32_t* status) {
+  const uint32_t lane = lane_id();
+  for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
+    const uint2 tile = tiles[t];
+    const uint32_t s = tile.y + lane;
+    if (lane >= tile_len(tile)) continue;
+    const uint2 kr = keyrank[s];
+    const uint32_t dst = start[kr.x] + kr.y;
+    if (dst >= total) { flag(status, kStatusRange); continue; }
+    tmp[dst] = __float_as_uint(pos[s].w);
+  }
+}
+
+// Order every bucket by particle index: the canonical (key, index) order.
+__global__ void k_ref_order(const uint2* __restrict__ tiles, uint32_t ntiles,
+                            const float4* __restrict__ pos,
+                            const uint2* __restrict__ keyrank,
+                            const uint32_t* __restrict__ start,
+                            const uint32_t* __restrict__ tmp,
+                            uint32_t* __restrict__ sorted) {
+  const uint32_t lane = lane_id();
+  for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
+    const uint2 tile = tiles[t];
+    const uint32_t s = tile.y + lane;
+    if (lane >= tile_len(tile)) continue;
+    const uint32_t key = keyrank[s].x;
+    const uint32_t id = __float_as_uint(pos[s].w);
+    const uint32_t b0 = start[key], b1 = start[key + 1];
+    uint32_t rank = 0;
+    for (uint32_t u = b0; u < b1; ++u) rank += tmp[u] < id ? 1u : 0u;
+    if (b0 + rank < b1) sorted[b0 + rank] = id;
+  }
+}
+
+// Per-slot debug intermediates of one scene to caller order.
 __global__ void k_export_debug(uint32_t first, uint32_t n,
                                const float4* __restrict__ pos,
-                               const uint32_t* __restrict__ dhash,
-                               const uint32_t* __restrict__ dkey,
                                const float4* __restrict__ accp,
                                const float4* __restrict__ velp,
                                const float4* __restrict__ velv,
-                               uint32_t* __restrict__ ohash,
-                               uint32_t* __restrict__ okey,
                                float* __restrict__ oaccp,
                                float* __restrict__ ovelp,
                                float* __restrict__ ovelv) {
@@ -782,8 +891,6 @@ __global__ void k_export_debug(uint32_t first, uint32_t n,
   const uint32_t s = first + k;
   const uint32_t id = __float_as_uint(pos[s].w);
   if (id >= n) return;
-  ohash[id] = dhash[s];
-  okey[id] = dkey[s];
   const float4 a = accp[s], b = velp[s], c = velv[s];
   oaccp[3 * id] = a.x; oaccp[3 * id + 1] = a.y; oaccp[3 * id + 2] = a.z;
   ovelp[3 * id] = b.x; ovelp[3 * id + 1] = b.y; ovelp[3 * id + 2] = b.z;
@@ -841,8 +948,8 @@ cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
   if (new_tiles.n) {
     k_reorder<<<grid_for(new_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
         new_tiles.d, new_tiles.n, c.scenes, c.tmp_hi, c.tmp_src, c.start, c.pos,
-        c.vel, c.pos2, c.vel2, c.pred, c.hash_s, c.cell_first, c.dbg_key,
-        c.src_limit, c.status);
+        c.vel, c.pos2, c.vel2, c.pred, c.hash_s, c.cell_first, c.src_limit,
+        c.status);
     k_cell_table<<<grid_for(new_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
         new_tiles.d, new_tiles.n, c.scenes, c.hash_s, c.cell_first, c.start,
         c.cell_tab);
@@ -912,15 +1019,35 @@ cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
 }
 
 cudaError_t launch_export_debug(uint32_t first, uint32_t n, const float4* pos,
-                                const uint32_t* dhash, const uint32_t* dkey,
                                 const float4* accp, const float4* velp,
-                                const float4* velv, uint32_t* ohash,
-                                uint32_t* okey, float* oaccp, float* ovelp,
+                                const float4* velv, float* oaccp, float* ovelp,
                                 float* ovelv, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  k_export_debug<<<(n + 255) / 256, 256, 0, st>>>(first, n, pos, dhash, dkey,
-                                                  accp, velp, velv, ohash, okey,
-                                                  oaccp, ovelp, ovelv);
+  k_export_debug<<<(n + 255) / 256, 256, 0, st>>>(first, n, pos, accp, velp,
+                                                  velv, oaccp, ovelp, ovelv);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ref_lookup(const LaunchCtx& c, const Tiles& new_tiles,
+                              uint32_t total, cudaStream_t st) {
+  if (new_tiles.n == 0) return cudaSuccess;
+  const uint32_t g = grid_for(new_tiles.n, c.block_misc, c.max_blocks);
+  k_ref_hash<<<g, c.block_misc, 0, st>>>(new_tiles.d, new_tiles.n, c.scenes,
+                                         c.pred, c.pos2, c.dbg_count,
+                                         c.dbg_keyrank, c.dbg_hash, c.dbg_key,
+                                         c.status);
+  LaunchCtx d = c;  // the scan over the lookup's own histogram
+  d.count = c.dbg_count;
+  d.start = c.dbg_start;
+  d.partial = c.dbg_partial;
+  cudaError_t e = launch_scan(d, total, st);
+  if (e != cudaSuccess) return e;
+  k_ref_scatter<<<g, c.block_misc, 0, st>>>(new_tiles.d, new_tiles.n, c.pos2,
+                                            c.dbg_keyrank, c.dbg_start, total,
+                                            c.dbg_tmp, c.status);
+  k_ref_order<<<g, c.block_misc, 0, st>>>(new_tiles.d, new_tiles.n, c.pos2,
+                                          c.dbg_keyrank, c.dbg_start, c.dbg_tmp,
+                                          c.dbg_sorted);
   return cudaGetLastError();
 }
 

@@ -47,12 +47,12 @@ struct LaunchCtx {
   float4* velp = nullptr;
   float2* dens_a = nullptr;
   float4* dens_b = nullptr;
-  uint4* keyrank = nullptr;   // (key, arrival rank, hash, id) per old slot
-  uint2* tmp_hi = nullptr;    // (hash, id) per bucketed slot
+  uint4* keyrank = nullptr;   // (key, arrival rank, cell, id) per old slot
+  uint2* tmp_hi = nullptr;    // (cell, id) per bucketed slot
   uint32_t* tmp_src = nullptr;  // source slot per bucketed slot
-  uint32_t* hash_s = nullptr;   // cell hash per sorted slot
+  uint32_t* hash_s = nullptr;   // internal cell index per sorted slot
   uint32_t* cell_first = nullptr;  // first slot of the particle's cell
-  uint2* cell_tab = nullptr;    // per cell (first slot): 27 (first, len) runs
+  uint2* cell_tab = nullptr;    // per cell (first slot): 9 rows x 3 runs
   uint32_t* count = nullptr;
   uint32_t* start = nullptr;
   uint32_t* partial = nullptr;
@@ -65,9 +65,17 @@ struct LaunchCtx {
                                 // (1: thread-per-particle walk)
   float4* out4 = nullptr;
   uint32_t* status = nullptr;
-  uint32_t* dbg_key = nullptr;
-  float4* dbg_accp = nullptr;
+  float4* dbg_accp = nullptr;   // captured substep: per-slot intermediates
   float4* dbg_velv = nullptr;
+  // captured substep: the reference's spatial lookup (launch_ref_lookup)
+  uint32_t* dbg_hash = nullptr;     // HashCell per particle (base + index)
+  uint32_t* dbg_key = nullptr;      // hash % n per particle (base + index)
+  uint32_t* dbg_count = nullptr;    // key histogram (zero between uses)
+  uint32_t* dbg_start = nullptr;    // startIndices as slot offsets
+  uint32_t* dbg_partial = nullptr;  // scan partials
+  uint2* dbg_keyrank = nullptr;     // (key, arrival rank) per slot
+  uint32_t* dbg_tmp = nullptr;      // bucketed particle indices
+  uint32_t* dbg_sorted = nullptr;   // (key, index)-ordered particle indices
   uint32_t src_limit = 0;  // slots of the layout a substep reads
   int block_misc = 256;   // predict/scatter/reorder
   int block_nbr = 128;    // list-based force kernels
@@ -107,11 +115,14 @@ cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
                           float* ovel, float* odens, uint32_t* oids,
                           cudaStream_t st);
 cudaError_t launch_export_debug(uint32_t first, uint32_t n, const float4* pos,
-                                const uint32_t* dhash, const uint32_t* dkey,
                                 const float4* accp, const float4* velp,
-                                const float4* velv, uint32_t* ohash,
-                                uint32_t* okey, float* oaccp, float* ovelp,
+                                const float4* velv, float* oaccp, float* ovelp,
                                 float* ovelv, cudaStream_t st);
+// The reference's spatial lookup of the substep being launched (after its
+// sort): k_ref_hash, the scan, k_ref_scatter, k_ref_order into the dbg_*
+// buffers of `c`.
+cudaError_t launch_ref_lookup(const LaunchCtx& c, const Tiles& new_tiles,
+                              uint32_t total, cudaStream_t st);
 cudaError_t launch_import(uint32_t first, uint32_t n, const float* ipos,
                           const float* ivel, float4* pos, float4* vel,
                           cudaStream_t st);

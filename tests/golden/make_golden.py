@@ -79,6 +79,16 @@ def edge_scenes():
                             **scenes.DAM_CONSTANTS)
     add("n2000_r0175", rng.uniform(-1.2, 1.2, (2000, 3)),
         rng.uniform(-0.5, 0.5, (2000, 3)), params=grav, dt=1.0 / 240.0)
+    # A box 40,000 cells long (r 0.05): a cell grid over it has to wrap, so
+    # two clusters 32768 cells apart along x land on the same cell indices
+    # of a 32768-cell grid row -- far cells in one bucket, as HashCell
+    # collisions put them in the reference.
+    wide = scenes.SimParams(radius=0.05, bound=(2000.0, 4.0, 4.0),
+                            **scenes.DAM_CONSTANTS)
+    a = rng.uniform(-0.15, 0.15, (300, 3)) + np.array([-799.9, 0.0, 0.0])
+    b = rng.uniform(-0.15, 0.15, (300, 3)) + np.array([-799.9 + 32768 * 0.05, 0.05, 0.0])
+    add("wrapped_grid", np.concatenate([a, b]), rng.uniform(-0.2, 0.2, (600, 3)),
+        params=wide, dt=1.0 / 240.0)
     return out
 
 
