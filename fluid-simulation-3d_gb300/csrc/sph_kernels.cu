@@ -61,6 +61,25 @@ __device__ __forceinline__ void flag(uint32_t* status, uint32_t f) {
   atomicOr(status, f);
 }
 
+// Entry k of slot i's neighbour list, k-major (entry k of all slots, then
+// entry k + 1), so a warp's appends and loads of one entry are contiguous.
+// 64-bit: k * stride passes 2^32 for capacities above 2^26.
+__device__ __forceinline__ uint64_t nbr_index(uint32_t i, uint32_t k,
+                                              uint32_t stride) {
+  return static_cast<uint64_t>(k) * stride + i;
+}
+
+// kGather consecutive entries of slot i's list from entry k0.
+template <int kGather>
+__device__ __forceinline__ void load_nbr_batch(const uint32_t* __restrict__ nbr,
+                                               uint32_t i, uint32_t k0,
+                                               uint32_t stride,
+                                               uint32_t (&j)[kGather]) {
+  const uint32_t* p = nbr + nbr_index(i, k0, stride);
+#pragma unroll
+  for (int u = 0; u < kGather; ++u) j[u] = __ldg(p + static_cast<uint64_t>(u) * stride);
+}
+
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
   const uint32_t lane = lane_id();
 #pragma unroll
@@ -441,9 +460,10 @@ __global__ void k_density_walk(const uint2* __restrict__ tiles,
     const uint32_t i = tile.y + lane;
     const float4 me = pred[i];
     const float3 p = make_float3(me.x, me.y, me.z);
-    uint32_t* row = nbr + i;
     float s2 = S.r2, s3 = S.r2 * S.r;  // self: w = r
     uint32_t cnt = 0;
+    uint32_t* wp = nbr + i;  // next list entry (a bumped pointer is the
+                             // cheapest append in the hit path)
     walk_runs(cell_tab, cell_first[i], pred, [&](uint32_t j, float4 q) {
       const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
       const float d2f = dist2_fast(dx, dy, dz);
@@ -455,7 +475,10 @@ __global__ void k_density_walk(const uint2* __restrict__ tiles,
           in_le = d2 <= S.cut_le;
         }
         if (in_le) {
-          if (cnt < nbr_cap) row[cnt * nbr_stride] = j;
+          if (cnt < nbr_cap) {
+            *wp = j;
+            wp += nbr_stride;
+          }
           ++cnt;
         }
         if (in_lt) density_pair(S, d2f, s2, s3);
@@ -544,7 +567,7 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
             const uint32_t hm = __ballot_sync(kFull, hit);
             if (hit) {
               const uint32_t k = base + __popc(hm & lt_mask);
-              if (k < nbr_cap) nbr[k * nbr_stride + ip] = js[c];
+              if (k < nbr_cap) nbr[nbr_index(ip, k, nbr_stride)] = js[c];
             }
             base += __popc(hm);
           }
@@ -554,18 +577,17 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
     }
     if (!live) continue;
     const float3 p = make_float3(me.x, me.y, me.z);
-    uint32_t* row = nbr + i;
     // phase 2: exact classification and the density sums
     float s2 = S.r2, s3 = S.r2 * S.r;  // self: w = r
     if (cnt <= nbr_cap) {
       uint32_t kept = 0;
       for (uint32_t k = 0; k < cnt; ++k) {
-        const uint32_t j = row[k * nbr_stride];
+        const uint32_t j = nbr[nbr_index(i, k, nbr_stride)];
         const float4 q = __ldg(pred + j);
         const float d2 = dist2(q.x - p.x, q.y - p.y, q.z - p.z);
         if (d2 <= S.cut_lt) density_pair(S, d2, s2, s3);
         if (d2 <= S.cut_le) {
-          if (kept != k) row[kept * nbr_stride] = j;
+          if (kept != k) nbr[nbr_index(i, kept, nbr_stride)] = j;
           ++kept;
         }
       }
@@ -641,13 +663,15 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
     float3 f = make_float3(0.0f, 0.0f, 0.0f);
     const uint32_t cnt = ncount[i];
     if (cnt <= nbr_cap) {
-      const uint32_t* row = nbr + i;
+      uint32_t jn[kGather];
+      if (cnt) load_nbr_batch<kGather>(nbr, i, 0, nbr_stride, jn);
       for (uint32_t k0 = 0; k0 < cnt; k0 += kGather) {
         uint32_t j[kGather];
         float4 q[kGather], b[kGather];
 #pragma unroll
-        for (int u = 0; u < kGather; ++u)
-          j[u] = (k0 + u < cnt) ? __ldg(row + (k0 + u) * nbr_stride) : i;
+        for (int u = 0; u < kGather; ++u) j[u] = (k0 + u < cnt) ? jn[u] : i;
+        // the next batch's entries load while this batch's gathers fly
+        if (k0 + kGather < cnt) load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, jn);
 #pragma unroll
         for (int u = 0; u < kGather; ++u) {
           q[u] = __ldg(pred + j[u]);
@@ -719,13 +743,15 @@ __global__ void k_visc_integrate(
       float3 f = make_float3(0.0f, 0.0f, 0.0f);
       const uint32_t cnt = ncount[i];
       if (cnt <= nbr_cap) {
-        const uint32_t* row = nbr + i;
+        uint32_t jn[kGather];
+        if (cnt) load_nbr_batch<kGather>(nbr, i, 0, nbr_stride, jn);
         for (uint32_t k0 = 0; k0 < cnt; k0 += kGather) {
           uint32_t j[kGather];
           float4 q[kGather], vj[kGather];
 #pragma unroll
-          for (int u = 0; u < kGather; ++u)
-            j[u] = (k0 + u < cnt) ? __ldg(row + (k0 + u) * nbr_stride) : i;
+          for (int u = 0; u < kGather; ++u) j[u] = (k0 + u < cnt) ? jn[u] : i;
+          if (k0 + kGather < cnt)
+            load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, jn);
 #pragma unroll
           for (int u = 0; u < kGather; ++u) {
             q[u] = __ldg(pred + j[u]);
