@@ -321,16 +321,14 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
 }
 
 // -------------------------------------------------------------- cell table
-// The run of cell index `cell` in its key bucket. A bucket is sorted by cell
-// index, so the cell's particles are one run and entries of other cells
-// that share the bucket are left out, as the reference's float(hash) test
-// leaves them out (:346); a bucket holding a single cell is the common case
-// and is recognised from its first and last entries.
-__device__ __forceinline__ uint2 bucket_run(const SceneDev& S, uint32_t cell,
-                                            const uint32_t* __restrict__ hash_s,
-                                            const uint32_t* __restrict__ start) {
-  const uint32_t key = S.base + fastmod(cell, S.fm, S.n);
-  const uint32_t b0 = __ldg(start + key), b1 = __ldg(start + key + 1);
+// The run of cell index `cell` in its key bucket [b0, b1). A bucket is
+// sorted by cell index, so the cell's particles are one run and entries of
+// other cells that share the bucket are left out, as the reference's
+// float(hash) test leaves them out (:346); a bucket holding a single cell is
+// the common case and is recognised from its first and last entries.
+__device__ __forceinline__ uint2 bucket_run(uint32_t cell, uint32_t b0,
+                                            uint32_t b1,
+                                            const uint32_t* __restrict__ hash_s) {
   uint32_t first = b0, len = 0;
   if (b1 > b0) {
     const uint32_t h0 = __ldg(hash_s + b0), h1 = __ldg(hash_s + b1 - 1);
@@ -352,13 +350,18 @@ __device__ __forceinline__ uint2 bucket_run(const SceneDev& S, uint32_t cell,
 // cell indices, hence consecutive keys; when their runs are adjacent in the
 // layout (their buckets hold no other cell -- the usual case inside the box)
 // the row is stored as one run flagged kRunMerged. Lanes take (cell, row)
-// pairs of the warp's tile in parallel.
-__global__ void k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
-                             const SceneDev* __restrict__ scenes,
-                             const uint32_t* __restrict__ hash_s,
-                             const uint32_t* __restrict__ cell_first,
-                             const uint32_t* __restrict__ start,
-                             uint2* __restrict__ cell_tab) {
+// pairs of the warp's tile in parallel; the warp's cell leaders are listed
+// in shared memory (kCellTableBlock threads per block).
+constexpr int kCellTableBlock = 256;
+
+__global__ void __launch_bounds__(kCellTableBlock)
+k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
+             const SceneDev* __restrict__ scenes,
+             const uint32_t* __restrict__ hash_s,
+             const uint32_t* __restrict__ cell_first,
+             const uint32_t* __restrict__ start, uint2* __restrict__ cell_tab) {
+  __shared__ uint8_t s_lead[kCellTableBlock / 32][32];
+  uint8_t* lead = s_lead[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -367,17 +370,30 @@ __global__ void k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
     const bool live = lane < tile_len(tile);
     const bool leader = live && cell_first[i] == i;
     const uint32_t lmask = __ballot_sync(kFull, leader);
+    if (leader) lead[__popc(lmask & ((1u << lane) - 1u))] = static_cast<uint8_t>(lane);
+    __syncwarp();
     const uint32_t pairs = __popc(lmask) * 9u;
+    const uint32_t kmax = fastmod(0xffffffffu, S.fm, S.n);  // key of 2^32 - 1
     for (uint32_t q = lane; q < pairs; q += 32) {
       const uint32_t c = q / 9u, w = q - c * 9u;
-      const int L = __fns(lmask, 0, static_cast<int>(c) + 1);
-      const uint32_t slot = tile.y + static_cast<uint32_t>(L);
+      const uint32_t slot = tile.y + lead[c];
       const uint32_t dy = w / 3u - 1u, dz = w % 3u - 1u;  // mod 2^32
       const uint32_t mid = __ldg(hash_s + slot) + dy * S.gwy + dz * S.gwz;
+      // keys of mid - 1, mid, mid + 1: neighbours of mid's key modulo n,
+      // except across the 2^32 wrap of the index
+      const uint32_t km = fastmod(mid, S.fm, S.n);
+      const uint32_t kl = mid == 0u ? kmax : (km == 0u ? S.n - 1u : km - 1u);
+      const uint32_t kh = mid == 0xffffffffu ? 0u : (km + 1u == S.n ? 0u : km + 1u);
+      const uint32_t* st = start + S.base;
+      const uint32_t l0 = __ldg(st + kl), l1 = __ldg(st + kl + 1);
+      const uint32_t m0 = kl + 1u == km ? l1 : __ldg(st + km);
+      const uint32_t m1 = __ldg(st + km + 1);
+      const uint32_t h0 = kh == km + 1u ? m1 : __ldg(st + kh);
+      const uint32_t h1 = __ldg(st + kh + 1);
       uint2 run[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-        run[k] = bucket_run(S, mid + static_cast<uint32_t>(k - 1), hash_s, start);
+      run[0] = bucket_run(mid - 1u, l0, l1, hash_s);
+      run[1] = bucket_run(mid, m0, m1, hash_s);
+      run[2] = bucket_run(mid + 1u, h0, h1, hash_s);
       uint32_t f = 0, e = 0;
       bool any = false, adjacent = true;
 #pragma unroll
@@ -404,6 +420,7 @@ __global__ void k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
         out[2] = run[2];
       }
     }
+    __syncwarp();  // the next tile rewrites the leader list
   }
 }
 
@@ -976,9 +993,10 @@ cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
         new_tiles.d, new_tiles.n, c.scenes, c.tmp_hi, c.tmp_src, c.start, c.pos,
         c.vel, c.pos2, c.vel2, c.pred, c.hash_s, c.cell_first, c.src_limit,
         c.status);
-    k_cell_table<<<grid_for(new_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
-        new_tiles.d, new_tiles.n, c.scenes, c.hash_s, c.cell_first, c.start,
-        c.cell_tab);
+    k_cell_table<<<grid_for(new_tiles.n, kCellTableBlock, c.max_blocks),
+                   kCellTableBlock, 0, st>>>(new_tiles.d, new_tiles.n, c.scenes,
+                                             c.hash_s, c.cell_first, c.start,
+                                             c.cell_tab);
   }
   return cudaGetLastError();
 }
