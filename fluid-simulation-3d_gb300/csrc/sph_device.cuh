@@ -6,7 +6,8 @@
 //   pred[P]             float4 (predicted position, cell index as raw bits)
 //   dens_a[P]           float2 (density, near density)
 //   dens_b[P]           float4 (1/rho, P/rho, 1/rho_n, Pn/rho_n)
-//   velp[P]             float4 post-pressure velocity (Jacobi snapshot)
+//   rec_v[2P]           32-byte records (pred, post-pressure velocity): the
+//                       Jacobi snapshot the viscosity pass reads
 //   keyrank[P]          uint4 (global key, arrival rank in the key bucket,
 //                       cell index, particle index)
 //   tmp_hi[P], tmp_src[P] bucketed (cell index, particle index) and source

@@ -106,7 +106,7 @@ Engine::~Engine() {
   if (join_out_) cudaEventDestroy(join_out_);
   if (work_) cudaStreamDestroy(work_);
   void* ptrs[] = {d_scenes_, d_tiles_old_, d_tiles_new_, d_pos_[0], d_pos_[1],
-                  d_vel_[0], d_vel_[1], ctx_.pred, ctx_.velp, ctx_.dens_a,
+                  d_vel_[0], d_vel_[1], ctx_.pred, ctx_.rec_v, ctx_.dens_a,
                   ctx_.dens_b, ctx_.keyrank, ctx_.tmp_hi, ctx_.tmp_src, ctx_.hash_s,
                   ctx_.nbr, ctx_.ncount, ctx_.cell_first, ctx_.cell_tab,
                   ctx_.count, ctx_.start,
@@ -160,7 +160,7 @@ int Engine::Init() {
     chk(Alloc(&d_vel_[b], C));
   }
   chk(Alloc(&ctx_.pred, C));
-  chk(Alloc(&ctx_.velp, C));
+  chk(Alloc(&ctx_.rec_v, 2 * C));
   chk(Alloc(&ctx_.dens_a, C));
   chk(Alloc(&ctx_.dens_b, C));
   chk(Alloc(&ctx_.keyrank, C));
@@ -196,7 +196,7 @@ int Engine::Init() {
 
 uint64_t Engine::BytesPerParticle() {
   return 2 * 2 * sizeof(float4)                // pos, vel (double-buffered)
-         + 2 * sizeof(float4)                  // pred, velp
+         + sizeof(float4) + 2 * sizeof(float4)  // pred, rec_v
          + sizeof(float2) + sizeof(float4)     // dens_a, dens_b
          + sizeof(uint4)                       // keyrank
          + sizeof(uint2) + 4 * sizeof(uint32_t)  // tmp_hi, tmp_src, hash_s,
@@ -301,7 +301,7 @@ int Engine::Load(uint32_t id, const float* pos3, const float* vel3,
     // Stage through the prediction / post-pressure buffers (rewritten by
     // every substep before use).
     float* sp = reinterpret_cast<float*>(ctx_.pred);
-    float* sv = reinterpret_cast<float*>(ctx_.velp);
+    float* sv = reinterpret_cast<float*>(ctx_.rec_v);
     SPH_CUDA(cudaMemcpyAsync(sp, pos3, sizeof(float) * 3 * n,
                              cudaMemcpyHostToDevice, st), "upload positions");
     if (vel3)
@@ -428,8 +428,9 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
                                 ss + 1 == substeps ? 1 : 0, st);
     mark(5);
     if (e == cudaSuccess && dbg)
-      e = cudaMemcpyAsync(d_dbg_velp_, c.velp, sizeof(float4) * total_,
-                          cudaMemcpyDeviceToDevice, st);
+      e = cudaMemcpy2DAsync(d_dbg_velp_, sizeof(float4), c.rec_v + 1,
+                            2 * sizeof(float4), sizeof(float4), total_,
+                            cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return CudaFail(e, "substep launch");
     cur = 1 - cur;
   }
@@ -544,9 +545,9 @@ int Engine::Download(uint32_t id, float* pos3, float* vel3, float* dens2,
   const uint32_t b = old_base_[id];
   float *op = pos3, *ov = vel3, *od = dens2;
   // Host copies stage through the prediction / post-pressure / density
-  // buffers (16 B per slot, rewritten by every substep before use).
+  // buffers (16-32 B per slot, rewritten by every substep before use).
   float* scratch = reinterpret_cast<float*>(ctx_.pred);
-  float* scratch_v = reinterpret_cast<float*>(ctx_.velp);
+  float* scratch_v = reinterpret_cast<float*>(ctx_.rec_v);
   float* scratch_d = reinterpret_cast<float*>(ctx_.dens_b);
   if (!device_ptrs) {
     op = pos3 ? scratch : nullptr;

@@ -69,6 +69,24 @@ __device__ __forceinline__ uint64_t nbr_index(uint32_t i, uint32_t k,
   return static_cast<uint64_t>(k) * stride + i;
 }
 
+// 32-byte particle records (rec_v): two float4 halves that a neighbour
+// gather fetches with one 256-bit load from one sector.
+__device__ __forceinline__ void load_rec(const float4* __restrict__ rec,
+                                         uint32_t j, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y),
+        "=f"(b.z), "=f"(b.w)
+      : "l"(rec + 2ull * j));
+}
+__device__ __forceinline__ void store_rec(float4* __restrict__ rec, uint32_t i,
+                                          float4 a, float4 b) {
+  asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};"
+               :
+               : "l"(rec + 2ull * i), "f"(a.x), "f"(a.y), "f"(a.z), "f"(a.w),
+                 "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+               : "memory");
+}
+
 // kGather consecutive entries of slot i's list from entry k0.
 template <int kGather>
 __device__ __forceinline__ void load_nbr_batch(const uint32_t* __restrict__ nbr,
@@ -616,12 +634,7 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
         if (j != i && d2 <= S.cut_lt) density_pair(S, d2, s2, s3);
       });
     }
-    const float rho = s2 * S.vol2, rhon = s3 * S.vol3;
-    dens_a[i] = make_float2(rho, rhon);
-    const float ir = 1.0f / rho, irn = 1.0f / rhon;
-    const float P = (rho - S.rho0) * S.k, Pn = rhon * S.kn;
-    dens_b[i] = make_float4(ir, P * ir, irn, Pn * irn);
-    ncount[i] = cnt;
+    density_store(S, i, s2, s3, cnt, dens_a, dens_b, ncount);
   }
 }
 
@@ -665,7 +678,7 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
                            const uint32_t* __restrict__ ncount,
                            uint32_t nbr_stride, uint32_t nbr_cap,
                            const float4* __restrict__ vel,
-                           float4* __restrict__ velp,
+                           float4* __restrict__ rec_v,
                            float4* __restrict__ dbg_accp) {
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
@@ -709,7 +722,9 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
     const float inv_rho = 1.0f / di.x;
     const float ax = f.x * inv_rho, ay = f.y * inv_rho, az = f.z * inv_rho;
     const float4 v = vel[i];
-    velp[i] = make_float4(v.x + ax * S.dt, v.y + ay * S.dt, v.z + az * S.dt, 0.f);
+    // viscosity record rec_v[i] = (predicted position, post-pressure velocity)
+    store_rec(rec_v, i, pi,
+              make_float4(v.x + ax * S.dt, v.y + ay * S.dt, v.z + az * S.dt, 0.f));
     if (dbg_accp) dbg_accp[i] = make_float4(ax, ay, az, 0.0f);
   }
 }
@@ -740,7 +755,7 @@ __global__ void k_visc_integrate(
     const SceneDev* __restrict__ scenes, const float4* __restrict__ pred,
     const uint32_t* __restrict__ cell_first, const uint2* __restrict__ cell_tab,
     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ ncount,
-    uint32_t nbr_stride, uint32_t nbr_cap, const float4* __restrict__ velp,
+    uint32_t nbr_stride, uint32_t nbr_cap, const float4* __restrict__ rec_v,
     float4* __restrict__ pos, float4* __restrict__ vel,
     float4* __restrict__ out4, int fuse_next, uint32_t* __restrict__ count,
     uint4* __restrict__ keyrank, float4* __restrict__ dbg_velv,
@@ -754,9 +769,9 @@ __global__ void k_visc_integrate(
     bool bad = false;
     uint32_t key = 0, cell = 0, id = 0;
     if (live) {
-      const float4 pi = pred[i];
+      float4 pi, vi;
+      load_rec(rec_v, i, pi, vi);
       const float3 p = make_float3(pi.x, pi.y, pi.z);
-      const float4 vi = velp[i];
       float3 f = make_float3(0.0f, 0.0f, 0.0f);
       const uint32_t cnt = ncount[i];
       if (cnt <= nbr_cap) {
@@ -770,17 +785,14 @@ __global__ void k_visc_integrate(
           if (k0 + kGather < cnt)
             load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, jn);
 #pragma unroll
-          for (int u = 0; u < kGather; ++u) {
-            q[u] = __ldg(pred + j[u]);
-            vj[u] = __ldg(velp + j[u]);
-          }
+          for (int u = 0; u < kGather; ++u) load_rec(rec_v, j[u], q[u], vj[u]);
 #pragma unroll
           for (int u = 0; u < kGather; ++u)
             if (k0 + u < cnt) visc_pair(S, p, vi, q[u], vj[u], f);
         }
       } else {
         walk_runs(cell_tab, cell_first[i], pred, [&](uint32_t j, float4 q) {
-          if (j != i) visc_pair(S, p, vi, q, __ldg(velp + j), f);
+          if (j != i) visc_pair(S, p, vi, q, __ldg(rec_v + 2ull * j + 1), f);
         });
       }
       const float c = S.vscale * S.mu * S.dt;
@@ -1031,7 +1043,7 @@ cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
                                                            : k_pressure<4>;
   kern<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
       tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.dens_a,
-      c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap, c.vel2, c.velp,
+      c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap, c.vel2, c.rec_v,
       c.dbg_accp);
   return cudaGetLastError();
 }
@@ -1046,7 +1058,7 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                               : k_visc_integrate<4>;
   kern<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
       tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.nbr,
-      c.ncount, c.nbr_stride, c.nbr_cap, c.velp, c.pos2, c.vel2,
+      c.ncount, c.nbr_stride, c.nbr_cap, c.rec_v, c.pos2, c.vel2,
       write_out ? c.out4 : nullptr, fuse_next, c.count, c.keyrank, c.dbg_velv,
       c.status);
   return cudaGetLastError();

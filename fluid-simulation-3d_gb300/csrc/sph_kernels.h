@@ -44,9 +44,9 @@ struct LaunchCtx {
   float4* pos2 = nullptr;  // state B (written by the reorder)
   float4* vel2 = nullptr;
   float4* pred = nullptr;
-  float4* velp = nullptr;
+  float4* rec_v = nullptr;  // 2 per slot: (pred, post-pressure velocity)
   float2* dens_a = nullptr;
-  float4* dens_b = nullptr;
+  float4* dens_b = nullptr;  // (1/rho, P/rho, 1/rho_n, Pn/rho_n) per slot
   uint4* keyrank = nullptr;   // (key, arrival rank, cell, id) per old slot
   uint2* tmp_hi = nullptr;    // (cell, id) per bucketed slot
   uint32_t* tmp_src = nullptr;  // source slot per bucketed slot
