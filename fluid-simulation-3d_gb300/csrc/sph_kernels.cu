@@ -61,6 +61,17 @@ __device__ __forceinline__ void flag(uint32_t* status, uint32_t f) {
   atomicOr(status, f);
 }
 
+// Programmatic dependent launch: the substep kernels are launched with
+// programmatic stream serialisation (launch_pdl), so each one is scheduled
+// while its predecessor's last wave runs. Every such kernel starts here: it
+// lets its own successor be scheduled, then waits for its predecessor to
+// complete with its memory visible (a hardware dependency, not a spin), so
+// nothing is read early. Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Entry k of slot i's neighbour list, k-major (entry k of all slots, then
 // entry k + 1), so a warp's appends and loads of one entry are contiguous.
 // 64-bit: k * stride passes 2^32 for capacities above 2^26.
@@ -170,6 +181,7 @@ __global__ void k_predict_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
                                const float4* __restrict__ vel,
                                uint32_t* __restrict__ count,
                                uint4* __restrict__ keyrank) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -217,6 +229,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x,
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_reduce(const uint32_t* __restrict__ count, uint32_t len,
               uint32_t* __restrict__ partial) {
+  pdl_enter();
   const uint32_t b0 = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
   uint32_t s = 0;
 #pragma unroll
@@ -230,6 +243,7 @@ k_scan_reduce(const uint32_t* __restrict__ count, uint32_t len,
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_partials(uint32_t* __restrict__ partial, uint32_t nb,
                 uint32_t* __restrict__ start, uint32_t len) {
+  pdl_enter();
   uint32_t carry = 0;
   for (uint32_t c = 0; c < nb; c += kScanThreads) {
     const uint32_t i = c + threadIdx.x;
@@ -246,6 +260,7 @@ __global__ void __launch_bounds__(kScanThreads)
 k_scan_down(uint32_t* __restrict__ count, uint32_t len,
             const uint32_t* __restrict__ partial,
             uint32_t* __restrict__ start) {
+  pdl_enter();
   const uint32_t b0 = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
   uint32_t s = 0;
@@ -272,6 +287,7 @@ __global__ void k_scatter(const uint2* __restrict__ tiles, uint32_t ntiles,
                           const uint32_t* __restrict__ start, uint32_t total,
                           uint2* __restrict__ tmp_hi,
                           uint32_t* __restrict__ tmp_src, uint32_t* status) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -303,6 +319,7 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
                           uint32_t* __restrict__ hash_s,
                           uint32_t* __restrict__ cell_first,
                           uint32_t src_limit, uint32_t* status) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -378,6 +395,7 @@ k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
              const uint32_t* __restrict__ hash_s,
              const uint32_t* __restrict__ cell_first,
              const uint32_t* __restrict__ start, uint2* __restrict__ cell_tab) {
+  pdl_enter();
   __shared__ uint8_t s_lead[kCellTableBlock / 32][32];
   uint8_t* lead = s_lead[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
@@ -487,6 +505,7 @@ __global__ void k_density_walk(const uint2* __restrict__ tiles,
                                uint32_t* __restrict__ nbr,
                                uint32_t* __restrict__ ncount,
                                uint32_t nbr_stride, uint32_t nbr_cap) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -542,6 +561,7 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
                           uint32_t* __restrict__ nbr,
                           uint32_t* __restrict__ ncount, uint32_t nbr_stride,
                           uint32_t nbr_cap) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   const uint32_t lt_mask = (1u << lane) - 1u;
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
@@ -680,6 +700,7 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
                            const float4* __restrict__ vel,
                            float4* __restrict__ rec_v,
                            float4* __restrict__ dbg_accp) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -760,6 +781,7 @@ __global__ void k_visc_integrate(
     float4* __restrict__ out4, int fuse_next, uint32_t* __restrict__ count,
     uint4* __restrict__ keyrank, float4* __restrict__ dbg_velv,
     uint32_t* status) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -867,6 +889,7 @@ __global__ void k_ref_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
                            uint2* __restrict__ keyrank,
                            uint32_t* __restrict__ ohash,
                            uint32_t* __restrict__ okey, uint32_t* status) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -899,6 +922,7 @@ __global__ void k_ref_scatter(const uint2* __restrict__ tiles, uint32_t ntiles,
                               const uint32_t* __restrict__ start,
                               uint32_t total, uint32_t* __restrict__ tmp,
                               uint32_t* status) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -918,6 +942,7 @@ __global__ void k_ref_order(const uint2* __restrict__ tiles, uint32_t ntiles,
                             const uint32_t* __restrict__ start,
                             const uint32_t* __restrict__ tmp,
                             uint32_t* __restrict__ sorted) {
+  pdl_enter();
   const uint32_t lane = lane_id();
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
@@ -970,22 +995,43 @@ __global__ void k_import(uint32_t first, uint32_t n,
 }  // namespace
 
 // ------------------------------------------------------------- launchers
+// Substep kernels go out with programmatic stream serialisation: the next
+// kernel is scheduled during its predecessor's last wave and waits for it in
+// pdl_enter(), which hides the launch and ramp-up between the nine kernels
+// of a substep (inside a graph these become programmatic edges).
+template <class... KArgs, class... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), uint32_t grid, int block,
+                       cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(static_cast<unsigned>(block));
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 cudaError_t launch_predict_hash(const LaunchCtx& c, const Tiles& old_tiles,
                                 cudaStream_t st) {
   if (old_tiles.n == 0) return cudaSuccess;
-  k_predict_hash<<<grid_for(old_tiles.n, c.block_misc, c.max_blocks),
-                   c.block_misc, 0, st>>>(old_tiles.d, old_tiles.n, c.scenes,
-                                          c.pos, c.vel, c.count, c.keyrank);
-  return cudaGetLastError();
+  return launch_pdl(k_predict_hash, grid_for(old_tiles.n, c.block_misc, c.max_blocks),
+                    c.block_misc, st, old_tiles.d, old_tiles.n, c.scenes, c.pos,
+                    c.vel, c.count, c.keyrank);
 }
 
 cudaError_t launch_scan(const LaunchCtx& c, uint32_t len, cudaStream_t st) {
   const uint32_t nb = (len + kScanBlock - 1) / kScanBlock;
   if (nb == 0) return cudaSuccess;
-  k_scan_reduce<<<nb, kScanThreads, 0, st>>>(c.count, len, c.partial);
-  k_scan_partials<<<1, kScanThreads, 0, st>>>(c.partial, nb, c.start, len);
-  k_scan_down<<<nb, kScanThreads, 0, st>>>(c.count, len, c.partial, c.start);
-  return cudaGetLastError();
+  cudaError_t e = launch_pdl(k_scan_reduce, nb, kScanThreads, st, c.count, len, c.partial);
+  if (e == cudaSuccess)
+    e = launch_pdl(k_scan_partials, 1, kScanThreads, st, c.partial, nb, c.start, len);
+  if (e == cudaSuccess)
+    e = launch_pdl(k_scan_down, nb, kScanThreads, st, c.count, len, c.partial, c.start);
+  return e;
 }
 
 uint32_t scan_partials_needed(uint64_t len) {
@@ -995,22 +1041,22 @@ uint32_t scan_partials_needed(uint64_t len) {
 cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
                                 const Tiles& new_tiles, uint32_t total,
                                 cudaStream_t st) {
-  if (old_tiles.n) {
-    k_scatter<<<grid_for(old_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
-        old_tiles.d, old_tiles.n, c.keyrank, c.start, total, c.tmp_hi,
-        c.tmp_src, c.status);
+  cudaError_t e = cudaSuccess;
+  if (old_tiles.n)
+    e = launch_pdl(k_scatter, grid_for(old_tiles.n, c.block_misc, c.max_blocks),
+                   c.block_misc, st, old_tiles.d, old_tiles.n, c.keyrank, c.start,
+                   total, c.tmp_hi, c.tmp_src, c.status);
+  if (new_tiles.n && e == cudaSuccess) {
+    e = launch_pdl(k_reorder, grid_for(new_tiles.n, c.block_misc, c.max_blocks),
+                   c.block_misc, st, new_tiles.d, new_tiles.n, c.scenes, c.tmp_hi,
+                   c.tmp_src, c.start, c.pos, c.vel, c.pos2, c.vel2, c.pred,
+                   c.hash_s, c.cell_first, c.src_limit, c.status);
+    if (e == cudaSuccess)
+      e = launch_pdl(k_cell_table, grid_for(new_tiles.n, kCellTableBlock, c.max_blocks),
+                     kCellTableBlock, st, new_tiles.d, new_tiles.n, c.scenes,
+                     c.hash_s, c.cell_first, c.start, c.cell_tab);
   }
-  if (new_tiles.n) {
-    k_reorder<<<grid_for(new_tiles.n, c.block_misc, c.max_blocks), c.block_misc, 0, st>>>(
-        new_tiles.d, new_tiles.n, c.scenes, c.tmp_hi, c.tmp_src, c.start, c.pos,
-        c.vel, c.pos2, c.vel2, c.pred, c.hash_s, c.cell_first, c.src_limit,
-        c.status);
-    k_cell_table<<<grid_for(new_tiles.n, kCellTableBlock, c.max_blocks),
-                   kCellTableBlock, 0, st>>>(new_tiles.d, new_tiles.n, c.scenes,
-                                             c.hash_s, c.cell_first, c.start,
-                                             c.cell_tab);
-  }
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
@@ -1018,21 +1064,17 @@ cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_nbr;
   const uint32_t g = grid_for(tiles.n, b, c.max_blocks);
-  if (c.cell_tile <= 1) {
-    k_density_walk<<<g, b, 0, st>>>(tiles.d, tiles.n, c.scenes, c.pred,
-                                    c.cell_first, c.cell_tab, c.dens_a,
-                                    c.dens_b, c.nbr, c.ncount, c.nbr_stride,
-                                    c.nbr_cap);
-    return cudaGetLastError();
-  }
+  if (c.cell_tile <= 1)
+    return launch_pdl(k_density_walk, g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
+                      c.cell_first, c.cell_tab, c.dens_a, c.dens_b, c.nbr,
+                      c.ncount, c.nbr_stride, c.nbr_cap);
   auto kern = c.cell_tile <= 64    ? k_density<2>
               : c.cell_tile <= 128 ? k_density<4>
               : c.cell_tile <= 192 ? k_density<6>
                                    : k_density<8>;
-  kern<<<g, b, 0, st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.dens_a,
-      c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap);
-  return cudaGetLastError();
+  return launch_pdl(kern, g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
+                    c.cell_first, c.cell_tab, c.dens_a, c.dens_b, c.nbr,
+                    c.ncount, c.nbr_stride, c.nbr_cap);
 }
 
 cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
@@ -1041,11 +1083,10 @@ cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
   const int b = c.block_nbr;
   auto kern = c.gather == 2 ? k_pressure<2> : c.gather == 8 ? k_pressure<8>
                                                            : k_pressure<4>;
-  kern<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.dens_a,
-      c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap, c.vel2, c.rec_v,
-      c.dbg_accp);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
+                    tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab,
+                    c.dens_a, c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap,
+                    c.vel2, c.rec_v, c.dbg_accp);
 }
 
 cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
@@ -1056,12 +1097,11 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
   auto kern = c.gather == 2   ? k_visc_integrate<2>
               : c.gather == 8 ? k_visc_integrate<8>
                               : k_visc_integrate<4>;
-  kern<<<grid_for(tiles.n, b, c.max_blocks), b, 0, st>>>(
-      tiles.d, tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.nbr,
-      c.ncount, c.nbr_stride, c.nbr_cap, c.rec_v, c.pos2, c.vel2,
-      write_out ? c.out4 : nullptr, fuse_next, c.count, c.keyrank, c.dbg_velv,
-      c.status);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
+                    tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.nbr,
+                    c.ncount, c.nbr_stride, c.nbr_cap, c.rec_v, c.pos2, c.vel2,
+                    write_out ? c.out4 : nullptr, fuse_next, c.count, c.keyrank,
+                    c.dbg_velv, c.status);
 }
 
 cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
@@ -1088,23 +1128,21 @@ cudaError_t launch_ref_lookup(const LaunchCtx& c, const Tiles& new_tiles,
                               uint32_t total, cudaStream_t st) {
   if (new_tiles.n == 0) return cudaSuccess;
   const uint32_t g = grid_for(new_tiles.n, c.block_misc, c.max_blocks);
-  k_ref_hash<<<g, c.block_misc, 0, st>>>(new_tiles.d, new_tiles.n, c.scenes,
-                                         c.pred, c.pos2, c.dbg_count,
-                                         c.dbg_keyrank, c.dbg_hash, c.dbg_key,
-                                         c.status);
+  cudaError_t e = launch_pdl(k_ref_hash, g, c.block_misc, st, new_tiles.d,
+                             new_tiles.n, c.scenes, c.pred, c.pos2, c.dbg_count,
+                             c.dbg_keyrank, c.dbg_hash, c.dbg_key, c.status);
   LaunchCtx d = c;  // the scan over the lookup's own histogram
   d.count = c.dbg_count;
   d.start = c.dbg_start;
   d.partial = c.dbg_partial;
-  cudaError_t e = launch_scan(d, total, st);
-  if (e != cudaSuccess) return e;
-  k_ref_scatter<<<g, c.block_misc, 0, st>>>(new_tiles.d, new_tiles.n, c.pos2,
-                                            c.dbg_keyrank, c.dbg_start, total,
-                                            c.dbg_tmp, c.status);
-  k_ref_order<<<g, c.block_misc, 0, st>>>(new_tiles.d, new_tiles.n, c.pos2,
-                                          c.dbg_keyrank, c.dbg_start, c.dbg_tmp,
-                                          c.dbg_sorted);
-  return cudaGetLastError();
+  if (e == cudaSuccess) e = launch_scan(d, total, st);
+  if (e == cudaSuccess)
+    e = launch_pdl(k_ref_scatter, g, c.block_misc, st, new_tiles.d, new_tiles.n,
+                   c.pos2, c.dbg_keyrank, c.dbg_start, total, c.dbg_tmp, c.status);
+  if (e == cudaSuccess)
+    e = launch_pdl(k_ref_order, g, c.block_misc, st, new_tiles.d, new_tiles.n,
+                   c.pos2, c.dbg_keyrank, c.dbg_start, c.dbg_tmp, c.dbg_sorted);
+  return e;
 }
 
 cudaError_t launch_import(uint32_t first, uint32_t n, const float* ipos,
