@@ -516,7 +516,7 @@ int Engine::Step(int substeps, cudaStream_t st) {
     SPH_CUDA(cudaEventRecord(join_out_, work_), "cudaEventRecord");
     SPH_CUDA(cudaStreamWaitEvent(st, join_out_, 0), "cudaStreamWaitEvent");
     launches_ += static_cast<uint64_t>(kKernelsPredict) +
-                 static_cast<uint64_t>(kKernelsPerSubstep) * substeps;
+                 static_cast<uint64_t>(kernels_per_substep(total_)) * substeps;
     profiled_substeps_ = profile_ ? substeps : 0;
     if (substeps & 1) cur_ = 1 - cur_;
   }

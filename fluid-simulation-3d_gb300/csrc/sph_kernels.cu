@@ -203,6 +203,7 @@ __global__ void k_predict_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanBlock = kScanThreads * kScanItems;
+constexpr uint32_t kScanFoldBlocks = 4096;  // fold the partials scan up to here
 
 // Block-wide exclusive scan of one value per thread; returns the block total
 // through *total.
@@ -256,11 +257,23 @@ k_scan_partials(uint32_t* __restrict__ partial, uint32_t nb,
   if (threadIdx.x == 0) start[len] = carry;
 }
 
+// Down-sweep. With `fold` the block totals in `partial` are raw (no
+// k_scan_partials): each block sums the totals before it itself -- O(nb^2)
+// reads in all, so the launcher folds only up to kScanFoldBlocks blocks --
+// and the last block writes the grand total start[len].
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_down(uint32_t* __restrict__ count, uint32_t len,
-            const uint32_t* __restrict__ partial,
+            const uint32_t* __restrict__ partial, uint32_t nb, int fold,
             uint32_t* __restrict__ start) {
   pdl_enter();
+  uint32_t base;
+  if (fold) {
+    uint32_t s = 0;
+    for (uint32_t c = threadIdx.x; c < blockIdx.x; c += kScanThreads) s += partial[c];
+    block_excl_scan(s, &base);
+  } else {
+    base = partial[blockIdx.x];
+  }
   const uint32_t b0 = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
   uint32_t s = 0;
@@ -270,7 +283,7 @@ k_scan_down(uint32_t* __restrict__ count, uint32_t len,
     s += v[k];
   }
   uint32_t total;
-  uint32_t run = block_excl_scan(s, &total) + partial[blockIdx.x];
+  uint32_t run = block_excl_scan(s, &total) + base;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     if (b0 + k < len) {
@@ -279,6 +292,7 @@ k_scan_down(uint32_t* __restrict__ count, uint32_t len,
     }
     run += v[k];
   }
+  if (fold && blockIdx.x + 1 == nb && threadIdx.x == 0) start[len] = base + total;
 }
 
 // ----------------------------------------------------------------- scatter
@@ -333,10 +347,12 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
     const float4 v = vel_in[src];
     float3 vn, pr;
     predict(S, p, v, vn, pr);
-    const uint32_t cell = cell_index(S, pr);
+    // the cell index travelled with the entry: k_predict_hash (or the fused
+    // prediction) computed it from this same prediction
+    const uint32_t cell = me.x;
     const uint32_t key = S.base + fastmod(cell, S.fm, S.n);
     const uint32_t b0 = start[key], b1 = start[key + 1];
-    if (slot < b0 || slot >= b1 || cell != me.x) {
+    if (slot < b0 || slot >= b1) {
       flag(status, kStatusRange);
       continue;
     }
@@ -1026,12 +1042,19 @@ cudaError_t launch_predict_hash(const LaunchCtx& c, const Tiles& old_tiles,
 cudaError_t launch_scan(const LaunchCtx& c, uint32_t len, cudaStream_t st) {
   const uint32_t nb = (len + kScanBlock - 1) / kScanBlock;
   if (nb == 0) return cudaSuccess;
+  const int fold = nb <= kScanFoldBlocks ? 1 : 0;
   cudaError_t e = launch_pdl(k_scan_reduce, nb, kScanThreads, st, c.count, len, c.partial);
-  if (e == cudaSuccess)
+  if (e == cudaSuccess && !fold)
     e = launch_pdl(k_scan_partials, 1, kScanThreads, st, c.partial, nb, c.start, len);
   if (e == cudaSuccess)
-    e = launch_pdl(k_scan_down, nb, kScanThreads, st, c.count, len, c.partial, c.start);
+    e = launch_pdl(k_scan_down, nb, kScanThreads, st, c.count, len, c.partial, nb,
+                   fold, c.start);
   return e;
+}
+
+int kernels_per_substep(uint32_t keys) {
+  const uint32_t nb = (keys + kScanBlock - 1) / kScanBlock;
+  return nb <= kScanFoldBlocks ? 8 : 9;
 }
 
 uint32_t scan_partials_needed(uint64_t len) {

@@ -105,10 +105,10 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                                   int fuse_next, int write_out,
                                   cudaStream_t st);
 
-// Kernels launched by one substep (scan 3, scatter, reorder, cell table,
-// density, pressure, viscosity) and by the standalone prediction of a
-// step's first substep.
-constexpr int kKernelsPerSubstep = 9;
+// Kernels launched by one substep over a key table of `keys` entries (scan 2
+// or 3, scatter, reorder, cell table, density, pressure, viscosity), and by
+// the standalone prediction of a step's first substep.
+int kernels_per_substep(uint32_t keys);
 constexpr int kKernelsPredict = 1;
 cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
                           const float4* vel, const float2* dens, float* opos,
