@@ -48,6 +48,8 @@ ALG_BYTES = {
     "density": 44,        # pred 16 + start 4 in; dens_a 8 + dens_b 16 out
     "pressure": 76,       # pred 16, start 4, dens_a 8, dens_b 16, vel 16 in; velp 16 out
     "viscosity": 84,      # pred 16, start 4, velp 16, pos 16 in; pos 16 + vel 16 out
+    # (pred and velp travel together as the 32-byte rec_v record; its pred
+    # half is a copy, so it is not counted as compulsory)
 }
 SURVEY_BYTES_PER_SUBSTEP = 300  # idealised whole-substep traffic per particle
 PHASES = ["predict_hash", "spatial", "density", "pressure", "viscosity"]
@@ -73,6 +75,27 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The largest `x` of all ranks (the job lasts as long as its slowest
+    replica); `x` itself for one rank."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(n_local: int, steps: int, total_ms: float, world: int,
+                       device):
+    """Whole-job particle-steps/s of `world` independent replicas (weak
+    scaling): every rank advanced n_local particles `steps` times in its own
+    `total_ms`; returns (value, job ms = max over ranks)."""
+    job_ms = max_over_ranks(total_ms, world, device)
+    return world * n_local * steps / (job_ms / 1000.0), job_ms
 
 
 def peaks():
@@ -269,18 +292,15 @@ def run_native(args):
         wall = time.perf_counter() - wall0
         launches = sim.kernel_launches() - launches0
         total_ms = float(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)))
-        if world > 1:
-            t = torch.tensor([total_ms], device="cuda")
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-            total_ms = float(t.item())
         return total_ms, wall, launches, phase
 
     clocks = ClockSampler(local)
     clocks.start()
-    total_ms, wall, launches, _ = timed_pass(False)
+    rank_ms, wall, launches, _ = timed_pass(False)
     clk = clocks.stop()
-    value = world * n * args.steps / (total_ms / 1000.0)
+    value, total_ms = replica_throughput(n, args.steps, rank_ms, world, "cuda")
     prof_ms, _, _, phase = timed_pass(True)
+    prof_ms = max_over_ranks(prof_ms, world, "cuda")
     sim.profile_enable(False)
     assert sim.status() == 0, "device status flags raised"
 
@@ -303,11 +323,7 @@ def run_native(args):
         if check != 0:
             raise RuntimeError("download failed")
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
     e2e_value = world * n * e2e_steps / e2e_s
     sim_tuning = sim.tuning()
     sim.close()
@@ -381,7 +397,10 @@ def run_batched(args):
     import fluidsim
     from fluidsim import scenes
 
-    torch.cuda.set_device(0)
+    rank, _, local = dist_env()
+    if rank != 0:  # one GPU's form: under torchrun rank 0 alone runs it
+        return 0
+    torch.cuda.set_device(local)
     scs = scenes.batched_scenes(256)
     total = sum(s["pos"].shape[0] for s in scs)
     stream = torch.cuda.current_stream()
@@ -452,7 +471,10 @@ def run_served(args):
 
     from fluidsim import scenes, server
 
-    torch.cuda.set_device(0)
+    rank, _, local = dist_env()
+    if rank != 0:  # one GPU's form: under torchrun rank 0 alone runs it
+        return 0
+    torch.cuda.set_device(local)
     rng = np.random.default_rng(3)
     reqs, t = [], 0.0
     while True:
