@@ -170,6 +170,51 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# FP32 operations counted per pair test (the density pass's candidate test:
+# 3 subtractions + the 3-term distance, 1 compare) and per neighbour (density
+# term 5, pressure term 25, viscosity term 15, each with its own distance).
+FLOPS_PER_CANDIDATE = 9
+FLOPS_PER_NEIGHBOUR = 45 + 2 * 8
+
+
+def pair_stats(sc, sample=4096, seed=0):
+    """Mean candidates (particles of the 27 neighbour cells, self included)
+    and neighbours (other particles within r) per particle, over a seeded
+    sample of the scene's initial state."""
+    from scipy.spatial import cKDTree
+    pos = np.ascontiguousarray(sc["pos"], np.float32)
+    r = np.float32(sc["params"].radius)
+    cells = np.floor(pos / r).astype(np.int64)
+    lo = cells.min(axis=0) - 1
+    dims = cells.max(axis=0) - lo + 2
+    key = ((cells[:, 2] - lo[2]) * dims[1] + (cells[:, 1] - lo[1])) * dims[0] + (cells[:, 0] - lo[0])
+    uniq, counts = np.unique(key, return_counts=True)
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(pos.shape[0], min(sample, pos.shape[0]), replace=False)
+    cand = np.zeros(idx.shape[0], np.int64)
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                k = key[idx] + (dz * dims[1] + dy) * dims[0] + dx
+                at = np.clip(np.searchsorted(uniq, k), 0, uniq.shape[0] - 1)
+                cand += np.where(uniq[at] == k, counts[at], 0)
+    tree = cKDTree(pos.astype(np.float64))
+    nb = np.array([len(v) - 1 for v in tree.query_ball_point(pos[idx].astype(np.float64), float(r))])
+    return float(cand.mean()), float(nb.mean())
+
+
+def nominal_fp32_tflops(device=0):
+    """SMs x 128 FP32 lanes x 2 (FMA) x max SM clock: the CUDA-core peak."""
+    import torch
+    props = torch.cuda.get_device_properties(device)
+    try:
+        with open(ROOT / "MEASURED_PEAKS.json") as f:
+            mhz = float(json.load(f)["sm_max_mhz"])
+    except Exception:
+        mhz = 2070.0
+    return props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
 def load_workload(name):
     from fluidsim import scenes
     if name not in scenes.WORKLOADS:
@@ -266,8 +311,11 @@ def run_native(args):
         events between its kernel phases (phase_times); those event nodes
         drain the GPU between kernels (about 4% of a step), so the headline
         pass runs without them and a second pass of the same steps supplies
-        the per-kernel times."""
+        the per-kernel times. Both passes start from the scene's initial
+        state, so they time the same (deterministic) trajectory: the flow
+        changes the neighbour counts, and with them every kernel's cost."""
         sim.profile_enable(profiled)
+        sim.upload(sc["pos"], sc["vel"])
         for _ in range(args.warmup):
             sim.step_async(dt, S)
         torch.cuda.synchronize()
@@ -375,6 +423,21 @@ def run_native(args):
     }
     if clk:
         line["clocks"] = clk
+    try:
+        cand, nbrs = pair_stats(sc)
+        substeps_s = n * S * args.steps / (total_ms / 1000.0) / world  # per rank
+        flops = FLOPS_PER_CANDIDATE * cand + FLOPS_PER_NEIGHBOUR * nbrs
+        peak32 = nominal_fp32_tflops(local)
+        line["pairs"] = {
+            "candidates_per_particle": cand, "neighbours_per_particle": nbrs,
+            "measured_on": "4096 particles of the initial state",
+            "pair_tests_per_s": world * substeps_s * (cand + 2 * nbrs),
+            "fp32_flops_per_particle_substep": flops,
+            "fp32_tflops": world * substeps_s * flops / 1e12,
+            "fp32_frac": substeps_s * flops / 1e12 / peak32,
+            "fp32_peak_tflops": peak32, "fp32_peak_source": "nominal (SMs x 128 x 2 x max clock)"}
+    except Exception as e:  # scipy missing: leave the block out
+        print(f"pair statistics skipped: {e}", file=sys.stderr)
     if not args.no_cpu_baseline and world == 1:
         rate, steps, el, th = cpu_port_rate(sc, max_steps=4, budget_s=8.0)
         line["cpu_baseline"] = {

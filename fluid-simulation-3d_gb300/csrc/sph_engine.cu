@@ -386,6 +386,7 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
   c.block_nbr = tuning_.block;
   c.cell_tile = tuning_.cell_tile;
   c.gather = tuning_.gather;
+  c.pdl = !profile_;  // phase events between kernels need plain launches
   c.max_blocks = 0;
   c.src_limit = static_cast<uint32_t>(capacity_);
   int cur = cur_;

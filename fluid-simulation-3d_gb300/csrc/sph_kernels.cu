@@ -1016,7 +1016,7 @@ __global__ void k_import(uint32_t first, uint32_t n,
 // pdl_enter(), which hides the launch and ramp-up between the nine kernels
 // of a substep (inside a graph these become programmatic edges).
 template <class... KArgs, class... Args>
-cudaError_t launch_pdl(void (*kernel)(KArgs...), uint32_t grid, int block,
+cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), uint32_t grid, int block,
                        cudaStream_t st, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
@@ -1027,14 +1027,14 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), uint32_t grid, int block,
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
 cudaError_t launch_predict_hash(const LaunchCtx& c, const Tiles& old_tiles,
                                 cudaStream_t st) {
   if (old_tiles.n == 0) return cudaSuccess;
-  return launch_pdl(k_predict_hash, grid_for(old_tiles.n, c.block_misc, c.max_blocks),
+  return launch_pdl(c.pdl, k_predict_hash, grid_for(old_tiles.n, c.block_misc, c.max_blocks),
                     c.block_misc, st, old_tiles.d, old_tiles.n, c.scenes, c.pos,
                     c.vel, c.count, c.keyrank);
 }
@@ -1043,11 +1043,11 @@ cudaError_t launch_scan(const LaunchCtx& c, uint32_t len, cudaStream_t st) {
   const uint32_t nb = (len + kScanBlock - 1) / kScanBlock;
   if (nb == 0) return cudaSuccess;
   const int fold = nb <= kScanFoldBlocks ? 1 : 0;
-  cudaError_t e = launch_pdl(k_scan_reduce, nb, kScanThreads, st, c.count, len, c.partial);
+  cudaError_t e = launch_pdl(c.pdl, k_scan_reduce, nb, kScanThreads, st, c.count, len, c.partial);
   if (e == cudaSuccess && !fold)
-    e = launch_pdl(k_scan_partials, 1, kScanThreads, st, c.partial, nb, c.start, len);
+    e = launch_pdl(c.pdl, k_scan_partials, 1, kScanThreads, st, c.partial, nb, c.start, len);
   if (e == cudaSuccess)
-    e = launch_pdl(k_scan_down, nb, kScanThreads, st, c.count, len, c.partial, nb,
+    e = launch_pdl(c.pdl, k_scan_down, nb, kScanThreads, st, c.count, len, c.partial, nb,
                    fold, c.start);
   return e;
 }
@@ -1066,16 +1066,16 @@ cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
                                 cudaStream_t st) {
   cudaError_t e = cudaSuccess;
   if (old_tiles.n)
-    e = launch_pdl(k_scatter, grid_for(old_tiles.n, c.block_misc, c.max_blocks),
+    e = launch_pdl(c.pdl, k_scatter, grid_for(old_tiles.n, c.block_misc, c.max_blocks),
                    c.block_misc, st, old_tiles.d, old_tiles.n, c.keyrank, c.start,
                    total, c.tmp_hi, c.tmp_src, c.status);
   if (new_tiles.n && e == cudaSuccess) {
-    e = launch_pdl(k_reorder, grid_for(new_tiles.n, c.block_misc, c.max_blocks),
+    e = launch_pdl(c.pdl, k_reorder, grid_for(new_tiles.n, c.block_misc, c.max_blocks),
                    c.block_misc, st, new_tiles.d, new_tiles.n, c.scenes, c.tmp_hi,
                    c.tmp_src, c.start, c.pos, c.vel, c.pos2, c.vel2, c.pred,
                    c.hash_s, c.cell_first, c.src_limit, c.status);
     if (e == cudaSuccess)
-      e = launch_pdl(k_cell_table, grid_for(new_tiles.n, kCellTableBlock, c.max_blocks),
+      e = launch_pdl(c.pdl, k_cell_table, grid_for(new_tiles.n, kCellTableBlock, c.max_blocks),
                      kCellTableBlock, st, new_tiles.d, new_tiles.n, c.scenes,
                      c.hash_s, c.cell_first, c.start, c.cell_tab);
   }
@@ -1088,14 +1088,14 @@ cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
   const int b = c.block_nbr;
   const uint32_t g = grid_for(tiles.n, b, c.max_blocks);
   if (c.cell_tile <= 1)
-    return launch_pdl(k_density_walk, g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
+    return launch_pdl(c.pdl, k_density_walk, g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
                       c.cell_first, c.cell_tab, c.dens_a, c.dens_b, c.nbr,
                       c.ncount, c.nbr_stride, c.nbr_cap);
   auto kern = c.cell_tile <= 64    ? k_density<2>
               : c.cell_tile <= 128 ? k_density<4>
               : c.cell_tile <= 192 ? k_density<6>
                                    : k_density<8>;
-  return launch_pdl(kern, g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
+  return launch_pdl(c.pdl, kern, g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
                     c.cell_first, c.cell_tab, c.dens_a, c.dens_b, c.nbr,
                     c.ncount, c.nbr_stride, c.nbr_cap);
 }
@@ -1106,7 +1106,7 @@ cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
   const int b = c.block_nbr;
   auto kern = c.gather == 2 ? k_pressure<2> : c.gather == 8 ? k_pressure<8>
                                                            : k_pressure<4>;
-  return launch_pdl(kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
+  return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
                     tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab,
                     c.dens_a, c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap,
                     c.vel2, c.rec_v, c.dbg_accp);
@@ -1120,7 +1120,7 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
   auto kern = c.gather == 2   ? k_visc_integrate<2>
               : c.gather == 8 ? k_visc_integrate<8>
                               : k_visc_integrate<4>;
-  return launch_pdl(kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
+  return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
                     tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.nbr,
                     c.ncount, c.nbr_stride, c.nbr_cap, c.rec_v, c.pos2, c.vel2,
                     write_out ? c.out4 : nullptr, fuse_next, c.count, c.keyrank,
@@ -1151,7 +1151,7 @@ cudaError_t launch_ref_lookup(const LaunchCtx& c, const Tiles& new_tiles,
                               uint32_t total, cudaStream_t st) {
   if (new_tiles.n == 0) return cudaSuccess;
   const uint32_t g = grid_for(new_tiles.n, c.block_misc, c.max_blocks);
-  cudaError_t e = launch_pdl(k_ref_hash, g, c.block_misc, st, new_tiles.d,
+  cudaError_t e = launch_pdl(c.pdl, k_ref_hash, g, c.block_misc, st, new_tiles.d,
                              new_tiles.n, c.scenes, c.pred, c.pos2, c.dbg_count,
                              c.dbg_keyrank, c.dbg_hash, c.dbg_key, c.status);
   LaunchCtx d = c;  // the scan over the lookup's own histogram
@@ -1160,10 +1160,10 @@ cudaError_t launch_ref_lookup(const LaunchCtx& c, const Tiles& new_tiles,
   d.partial = c.dbg_partial;
   if (e == cudaSuccess) e = launch_scan(d, total, st);
   if (e == cudaSuccess)
-    e = launch_pdl(k_ref_scatter, g, c.block_misc, st, new_tiles.d, new_tiles.n,
+    e = launch_pdl(c.pdl, k_ref_scatter, g, c.block_misc, st, new_tiles.d, new_tiles.n,
                    c.pos2, c.dbg_keyrank, c.dbg_start, total, c.dbg_tmp, c.status);
   if (e == cudaSuccess)
-    e = launch_pdl(k_ref_order, g, c.block_misc, st, new_tiles.d, new_tiles.n,
+    e = launch_pdl(c.pdl, k_ref_order, g, c.block_misc, st, new_tiles.d, new_tiles.n,
                    c.pos2, c.dbg_keyrank, c.dbg_start, c.dbg_tmp, c.dbg_sorted);
   return e;
 }

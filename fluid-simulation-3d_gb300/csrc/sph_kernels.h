@@ -77,6 +77,8 @@ struct LaunchCtx {
   uint32_t* dbg_tmp = nullptr;      // bucketed particle indices
   uint32_t* dbg_sorted = nullptr;   // (key, index)-ordered particle indices
   uint32_t src_limit = 0;  // slots of the layout a substep reads
+  bool pdl = true;        // programmatic dependent launch (off while the
+                          // engine records phase events between kernels)
   int block_misc = 256;   // predict/scatter/reorder
   int block_nbr = 128;    // list-based force kernels
   uint32_t max_blocks = 0;  // persistent grid cap (0 = no cap)
