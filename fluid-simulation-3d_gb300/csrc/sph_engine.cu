@@ -384,6 +384,7 @@ int Engine::UploadScenes(int substeps, cudaStream_t st) {
 int Engine::RunSubsteps(int substeps, cudaStream_t st) {
   LaunchCtx c = ctx_;
   c.block_nbr = tuning_.block;
+  c.block_force = tuning_.force_block ? tuning_.force_block : tuning_.block;
   c.cell_tile = tuning_.cell_tile;
   c.gather = tuning_.gather;
   c.pdl = !profile_;  // phase events between kernels need plain launches
@@ -678,15 +679,19 @@ int Engine::SetTuning(const sph_tuning& t) {
     return Fail(SPH_ERR_INVALID, "cell_tile must be 1, 64, 128, 192 or 256");
   if (t.gather != 2 && t.gather != 4 && t.gather != 8)
     return Fail(SPH_ERR_INVALID, "gather must be 2, 4 or 8");
+  if (t.force_block != 0 &&
+      (t.force_block < 32 || t.force_block > 1024 || (t.force_block & 31)))
+    return Fail(SPH_ERR_INVALID, "force_block must be 0 or a multiple of 32 in [32, 1024]");
   if (t.block != tuning_.block || t.particles_per_warp != tuning_.particles_per_warp ||
-      t.cell_tile != tuning_.cell_tile || t.gather != tuning_.gather)
+      t.cell_tile != tuning_.cell_tile || t.gather != tuning_.gather ||
+      t.force_block != tuning_.force_block)
     ReleaseGraphs();
   tuning_ = t;
   return SPH_OK;
 }
 
-// Coordinate search: block size x cell tile at the current gather batch,
-// then the gather batch at the best of those.
+// Coordinate search: block size x cell tile (all neighbour kernels), then
+// the block size of the force kernels alone, then their gather batch.
 int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
                      float* best_ms, cudaStream_t st) {
   if (steps_per_trial < 1) return Fail(SPH_ERR_INVALID, "steps_per_trial >= 1");
@@ -696,15 +701,18 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
   SPH_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
   SPH_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
   int rc = SPH_OK;
-  for (int round = 0; round < 2 && rc == SPH_OK; ++round) {
+  for (int round = 0; round < 3 && rc == SPH_OK; ++round) {
     std::vector<sph_tuning> space;
     if (round == 0) {
       for (int b : {64, 128, 256, 512})
         for (int tile : {1, 64, 128, 256})
-          space.push_back(sph_tuning{b, tile, 32, tuning_.gather});
+          space.push_back(sph_tuning{b, tile, 32, tuning_.gather, 0});
+    } else if (round == 1) {
+      for (int fb : {64, 128, 256, 512})
+        space.push_back(sph_tuning{win.block, win.cell_tile, 32, win.gather, fb});
     } else {
       for (int g : {2, 4, 8})
-        space.push_back(sph_tuning{win.block, win.cell_tile, 32, g});
+        space.push_back(sph_tuning{win.block, win.cell_tile, 32, g, win.force_block});
     }
     for (const sph_tuning& t : space) {
       if ((rc = SetTuning(t)) != SPH_OK) break;

@@ -1103,7 +1103,7 @@ cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
 cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
                             cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
-  const int b = c.block_nbr;
+  const int b = c.block_force;
   auto kern = c.gather == 2 ? k_pressure<2> : c.gather == 8 ? k_pressure<8>
                                                            : k_pressure<4>;
   return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
@@ -1116,7 +1116,7 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                                   int fuse_next, int write_out,
                                   cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
-  const int b = c.block_nbr;
+  const int b = c.block_force;
   auto kern = c.gather == 2   ? k_visc_integrate<2>
               : c.gather == 8 ? k_visc_integrate<8>
                               : k_visc_integrate<4>;

@@ -80,7 +80,8 @@ struct LaunchCtx {
   bool pdl = true;        // programmatic dependent launch (off while the
                           // engine records phase events between kernels)
   int block_misc = 256;   // predict/scatter/reorder
-  int block_nbr = 128;    // list-based force kernels
+  int block_nbr = 128;    // neighbour kernels (density)
+  int block_force = 128;  // pressure and viscosity
   uint32_t max_blocks = 0;  // persistent grid cap (0 = no cap)
 };
 

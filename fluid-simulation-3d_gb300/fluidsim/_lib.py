@@ -56,7 +56,8 @@ class Params(ctypes.Structure):
 class Tuning(ctypes.Structure):
     """struct sph_tuning."""
     _fields_ = [("block", ctypes.c_int32), ("cell_tile", ctypes.c_int32),
-                ("particles_per_warp", ctypes.c_int32), ("gather", ctypes.c_int32)]
+                ("particles_per_warp", ctypes.c_int32), ("gather", ctypes.c_int32),
+                ("force_block", ctypes.c_int32)]
 
 
 _P = ctypes.c_void_p

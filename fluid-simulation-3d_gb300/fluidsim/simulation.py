@@ -204,15 +204,17 @@ class FluidSimulation:
     def kernel_launches(self) -> int:
         return int(self._lib.sph_kernel_launches(self._h))
 
-    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4):
-        t = Tuning(block, cell_tile, particles_per_warp, gather)
+    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4,
+                   force_block=0):
+        t = Tuning(block, cell_tile, particles_per_warp, gather, force_block)
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), self._h)
 
     def tuning(self):
         t = Tuning()
         check(self._lib.sph_get_tuning(self._h, ctypes.byref(t)), self._h)
         return dict(block=t.block, cell_tile=t.cell_tile,
-                    particles_per_warp=t.particles_per_warp, gather=t.gather)
+                    particles_per_warp=t.particles_per_warp, gather=t.gather,
+                    force_block=t.force_block)
 
     def autotune(self, deltatime, substeps=1, steps_per_trial=2):
         """Sweep the launch configuration on real steps (the state advances);
@@ -224,7 +226,8 @@ class FluidSimulation:
                                      ctypes.byref(ms), self._stream), self._h)
         self._cache = None
         return dict(block=t.block, cell_tile=t.cell_tile,
-                    particles_per_warp=t.particles_per_warp, gather=t.gather), float(ms.value)
+                    particles_per_warp=t.particles_per_warp, gather=t.gather,
+                    force_block=t.force_block), float(ms.value)
 
     @property
     def handle(self):
@@ -403,15 +406,17 @@ class Batch:
                                                  _ptr(dens), self._stream))
         return pos, vel, dens
 
-    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4):
-        t = Tuning(block, cell_tile, particles_per_warp, gather)
+    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4,
+                   force_block=0):
+        t = Tuning(block, cell_tile, particles_per_warp, gather, force_block)
         self._check(self._lib.sph_batch_set_tuning(self._h, ctypes.byref(t)))
 
     def tuning(self):
         t = Tuning()
         self._check(self._lib.sph_batch_get_tuning(self._h, ctypes.byref(t)))
         return dict(block=t.block, cell_tile=t.cell_tile,
-                    particles_per_warp=t.particles_per_warp, gather=t.gather)
+                    particles_per_warp=t.particles_per_warp, gather=t.gather,
+                    force_block=t.force_block)
 
     def autotune(self, substeps: int, steps_per_trial: int = 2):
         t = Tuning()
@@ -420,7 +425,8 @@ class Batch:
                                                  ctypes.byref(t), ctypes.byref(ms),
                                                  self._stream))
         return dict(block=t.block, cell_tile=t.cell_tile,
-                    particles_per_warp=t.particles_per_warp, gather=t.gather), float(ms.value)
+                    particles_per_warp=t.particles_per_warp, gather=t.gather,
+                    force_block=t.force_block), float(ms.value)
 
     def profile_enable(self, on=True):
         self._check(self._lib.sph_batch_profile_enable(self._h, 1 if on else 0))

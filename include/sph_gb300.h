@@ -68,6 +68,8 @@ typedef struct sph_tuning {
   int32_t particles_per_warp; /* particles per warp: 32 (one per lane)    */
   int32_t gather;     /* neighbour-list entries whose gathers the force
                          kernels issue together: 2, 4 or 8 (default 4)    */
+  int32_t force_block; /* threads per block of the pressure and viscosity
+                          kernels (multiple of 32, 32..1024); 0 = block   */
 } sph_tuning;
 
 /* Reference defaults of physicsWorld.h:96-106,145 and physicsWorld.cc:47,87. */
