@@ -98,7 +98,9 @@ __device__ __forceinline__ void store_rec(float4* __restrict__ rec, uint32_t i,
                : "memory");
 }
 
-// kGather consecutive entries of slot i's list from entry k0.
+// kGather consecutive entries of slot i's list from entry k0. Each entry is
+// read once per pass, so the loads carry the streaming (evict-first) hint
+// and leave the cache to the neighbours' gathered state.
 template <int kGather>
 __device__ __forceinline__ void load_nbr_batch(const uint32_t* __restrict__ nbr,
                                                uint32_t i, uint32_t k0,
@@ -106,7 +108,7 @@ __device__ __forceinline__ void load_nbr_batch(const uint32_t* __restrict__ nbr,
                                                uint32_t (&j)[kGather]) {
   const uint32_t* p = nbr + nbr_index(i, k0, stride);
 #pragma unroll
-  for (int u = 0; u < kGather; ++u) j[u] = __ldg(p + static_cast<uint64_t>(u) * stride);
+  for (int u = 0; u < kGather; ++u) j[u] = __ldcs(p + static_cast<uint64_t>(u) * stride);
 }
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
