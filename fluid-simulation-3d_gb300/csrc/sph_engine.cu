@@ -245,6 +245,7 @@ int Engine::AddScene(const sph_params& p, uint32_t n, const float* pos3,
   old_base_[s] = static_cast<uint32_t>(layout_total_);
   layout_total_ += n;
   layout_dirty_ = scenes_dirty_ = true;
+  carry_valid_ = false;
   const int rc = Load(s, pos3, vel3, device_ptrs, st);
   if (rc != SPH_OK) {
     sc = Scene{};
@@ -260,6 +261,7 @@ int Engine::RemoveScene(uint32_t id) {
     return Fail(SPH_ERR_INVALID, "no such scene");
   scenes_[id].live = false;  // its slots vanish at the next step's sort
   layout_dirty_ = scenes_dirty_ = true;
+  carry_valid_ = false;
   return SPH_OK;
 }
 
@@ -270,6 +272,7 @@ int Engine::SetParams(uint32_t id, const sph_params& p) {
     return Fail(SPH_ERR_INVALID, "radius must be positive and finite");
   scenes_[id].prm = p;
   scenes_dirty_ = true;
+  carry_valid_ = false;
   return SPH_OK;
 }
 
@@ -285,6 +288,7 @@ int Engine::SetDt(uint32_t id, float dt) {
   if (scenes_[id].dt != dt) {
     scenes_[id].dt = dt;
     scenes_dirty_ = true;
+    carry_valid_ = false;
   }
   return SPH_OK;
 }
@@ -295,6 +299,7 @@ int Engine::Load(uint32_t id, const float* pos3, const float* vel3,
     return Fail(SPH_ERR_INVALID, "no such scene");
   // pos3 == nullptr loads the zero state (InitializeData, physicsWorld.cc:129-137).
   const uint32_t n = scenes_[id].n;
+  carry_valid_ = false;  // a new state needs its own prediction
   const float* dp = pos3;
   const float* dv = vel3;
   if (!device_ptrs && pos3) {
@@ -381,7 +386,7 @@ int Engine::UploadScenes(int substeps, cudaStream_t st) {
 
 // Launches `substeps` substeps starting from state buffers cur_. Does not
 // change engine state, so it can run under stream capture.
-int Engine::RunSubsteps(int substeps, cudaStream_t st) {
+int Engine::RunSubsteps(int substeps, cudaStream_t st, bool carry) {
   LaunchCtx c = ctx_;
   c.block_nbr = tuning_.block;
   c.block_force = tuning_.force_block ? tuning_.force_block : tuning_.block;
@@ -415,7 +420,7 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
                     : cudaEventRecord(ev[k], st);
     };
     mark(0);
-    if (ss == 0) e = launch_predict_hash(c, first, st);
+    if (ss == 0 && !carry) e = launch_predict_hash(c, first, st);
     mark(1);
     if (e == cudaSuccess) e = launch_scan(c, total_, st);
     if (e == cudaSuccess) e = launch_sort_reorder(c, first, tnew, total_, st);
@@ -425,9 +430,10 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st) {
     mark(3);
     if (e == cudaSuccess) e = launch_pressure(c, tnew, st);
     mark(4);
+    // every viscosity pass predicts the following substep, the last one
+    // the next step's first (used when nothing changes in between)
     if (e == cudaSuccess)
-      e = launch_visc_integrate(c, tnew, ss + 1 < substeps ? 1 : 0,
-                                ss + 1 == substeps ? 1 : 0, st);
+      e = launch_visc_integrate(c, tnew, 1, ss + 1 == substeps ? 1 : 0, st);
     mark(5);
     if (e == cudaSuccess && dbg)
       e = cudaMemcpy2DAsync(d_dbg_velp_, sizeof(float4), c.rec_v + 1,
@@ -480,23 +486,34 @@ int Engine::Step(int substeps, cudaStream_t st) {
     return Fail(SPH_ERR_INVALID, "substeps must be in [1, 64]");
   if (debug_ && substeps != 1)
     return Fail(SPH_ERR_STATE, "debug capture needs substeps == 1");
+  // the previous step already predicted this step's first substep unless
+  // something changed since (checked before the layout and scene tables
+  // are refreshed)
+  const bool carry = carry_valid_ && !layout_dirty_ && !scenes_dirty_ &&
+                     uploaded_substeps_ == substeps && n_tiles_old_ == n_tiles_new_;
   int rc = BuildLayout(st);
   if (rc != SPH_OK) return rc;
   rc = UploadScenes(substeps, st);
   if (rc != SPH_OK) return rc;
+  if (!carry && count_extent_) {
+    // an unused carried prediction left its histogram behind
+    SPH_CUDA(cudaMemsetAsync(ctx_.count, 0, sizeof(uint32_t) * count_extent_, st),
+             "histogram reset");
+    count_extent_ = 0;
+  }
   if (total_ > 0) {
     // join: the work stream starts after everything queued on `st`
     SPH_CUDA(cudaEventRecord(join_in_, st), "cudaEventRecord");
     SPH_CUDA(cudaStreamWaitEvent(work_, join_in_, 0), "cudaStreamWaitEvent");
     const bool steady = n_tiles_old_ == n_tiles_new_ && !layout_dirty_;
     if (use_graphs_ && steady && !debug_) {
-      const auto key = std::make_pair(substeps, cur_);
+      const auto key = std::make_pair(substeps, cur_ + (carry ? 2 : 0));
       auto it = graphs_.find(key);
       if (it == graphs_.end()) {
         cudaGraph_t g = nullptr;
         SPH_CUDA(cudaStreamBeginCapture(work_, cudaStreamCaptureModeThreadLocal),
                  "cudaStreamBeginCapture");
-        rc = RunSubsteps(substeps, work_);
+        rc = RunSubsteps(substeps, work_, carry);
         const cudaError_t e = cudaStreamEndCapture(work_, &g);
         if (rc != SPH_OK) {
           if (g) cudaGraphDestroy(g);
@@ -511,14 +528,16 @@ int Engine::Step(int substeps, cudaStream_t st) {
       }
       SPH_CUDA(cudaGraphLaunch(it->second, work_), "cudaGraphLaunch");
     } else {
-      rc = RunSubsteps(substeps, work_);
+      rc = RunSubsteps(substeps, work_, carry);
       if (rc != SPH_OK) return rc;
     }
     // join back: later work on `st` sees the step's results
     SPH_CUDA(cudaEventRecord(join_out_, work_), "cudaEventRecord");
     SPH_CUDA(cudaStreamWaitEvent(st, join_out_, 0), "cudaStreamWaitEvent");
-    launches_ += static_cast<uint64_t>(kKernelsPredict) +
+    launches_ += static_cast<uint64_t>(carry ? 0 : kKernelsPredict) +
                  static_cast<uint64_t>(kernels_per_substep(total_)) * substeps;
+    carry_valid_ = true;
+    count_extent_ = total_;
     profiled_substeps_ = profile_ ? substeps : 0;
     if (substeps & 1) cur_ = 1 - cur_;
   }

@@ -76,7 +76,7 @@ class Engine {
   };
   int BuildLayout(cudaStream_t st);
   int UploadScenes(int substeps, cudaStream_t st);
-  int RunSubsteps(int substeps, cudaStream_t st);
+  int RunSubsteps(int substeps, cudaStream_t st, bool carry);
   void BuildTiles(std::vector<uint2>& out, bool old_layout) const;
   void ReleaseGraphs();
 
@@ -89,6 +89,13 @@ class Engine {
   bool layout_dirty_ = true;
   bool scenes_dirty_ = true;
   int uploaded_substeps_ = -1;
+  // The last substep of a step also predicts the next step's first substep
+  // (key, rank and histogram, fused in its viscosity pass). carry_valid_:
+  // nothing has changed since (state, settings, dt, layout), so the next
+  // step skips k_predict_hash. count_extent_: keys whose histogram entries
+  // that prediction wrote (cleared if it goes unused).
+  bool carry_valid_ = false;
+  uint32_t count_extent_ = 0;
 
   // device memory
   void* arena_ = nullptr;
@@ -130,7 +137,7 @@ class Engine {
   cudaStream_t work_ = nullptr;
   cudaEvent_t join_in_ = nullptr, join_out_ = nullptr;
 
-  // CUDA graphs, keyed by (substeps, state parity)
+  // CUDA graphs, keyed by (substeps, state parity + 2 * carried prediction)
   bool use_graphs_ = true;
   std::map<std::pair<int, int>, cudaGraphExec_t> graphs_;
 
