@@ -98,7 +98,6 @@ class Engine {
   uint32_t count_extent_ = 0;
 
   // device memory
-  void* arena_ = nullptr;
   SceneDev* d_scenes_ = nullptr;
   uint2* d_tiles_old_ = nullptr;
   uint2* d_tiles_new_ = nullptr;
