@@ -117,6 +117,18 @@ def ncu_traffic(workload, kernel):
         return None
 
 
+def ncu_issue(workload, kernel):
+    """Issue-slot use of a kernel from the same ncu summary: percent of
+    cycles with an instruction issued, active lanes per instruction and warp
+    instructions per particle (what bounds a kernel that is not HBM-bound)."""
+    try:
+        with open(ROOT / "profiles" / "dram_traffic.json") as f:
+            d = json.load(f)
+        return d["issue"][workload][kernel]
+    except Exception:
+        return None
+
+
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed
     region."""
@@ -411,7 +423,8 @@ def run_native(args):
                      "traffic": (tr * n if tr is not None else None),
                      "timing": "CUDA events around each kernel phase on the "
                                "library's stream, over a second pass of the "
-                               "same steps (profiled_ms_per_step)"},
+                               "same steps (profiled_ms_per_step)",
+                     "issue": ncu_issue(args.workload, dom)},
         "profiled_ms_per_step": prof_ms / args.steps,
         "substep": {"ms": sub_ms,
                     "alg_GBps_at_300B": SURVEY_BYTES_PER_SUBSTEP * n / (sub_ms / 1000) / 1e9,
