@@ -231,25 +231,40 @@ int Engine::AddScene(const sph_params& p, uint32_t n, const float* pos3,
     return Fail(SPH_ERR_INVALID, "scene size must be in [1, 2^24)");
   if (!(p.radius > 0.0f) || !std::isfinite(p.radius))
     return Fail(SPH_ERR_INVALID, "radius must be positive and finite");
-  if (layout_total_ + n > capacity_)
+  // where the scene goes in the current layout: the first free extent that
+  // holds it, else past the end
+  size_t fi = 0;
+  while (fi < free_.size() && free_[fi].second < n) ++fi;
+  const bool in_gap = fi < free_.size();
+  if (!in_gap && layout_total_ + n > capacity_)
     return Fail(SPH_ERR_NOMEM, "scene does not fit the engine capacity");
   uint32_t s = 0;
   while (s < max_scenes_ && scenes_[s].used) ++s;
   if (s == max_scenes_) return Fail(SPH_ERR_NOMEM, "no free scene slot");
+  const uint64_t base = in_gap ? free_[fi].first : layout_total_;
+  if (in_gap) {
+    free_[fi].first += n;
+    free_[fi].second -= n;
+    if (free_[fi].second == 0) free_.erase(free_.begin() + static_cast<std::ptrdiff_t>(fi));
+  } else {
+    layout_total_ += n;
+  }
   Scene& sc = scenes_[s];
   sc = Scene{};
   sc.used = sc.live = true;
   sc.prm = p;
   sc.n = n;
   sc.dt = dt;
-  old_base_[s] = static_cast<uint32_t>(layout_total_);
-  layout_total_ += n;
+  old_base_[s] = static_cast<uint32_t>(base);
   layout_dirty_ = scenes_dirty_ = true;
   carry_valid_ = false;
   const int rc = Load(s, pos3, vel3, device_ptrs, st);
   if (rc != SPH_OK) {
     sc = Scene{};
-    layout_total_ -= n;
+    if (base + n == layout_total_)
+      layout_total_ -= n;
+    else
+      free_.emplace_back(base, n);
     return rc;
   }
   if (id) *id = s;
@@ -262,6 +277,14 @@ int Engine::RemoveScene(uint32_t id) {
   scenes_[id].live = false;  // its slots vanish at the next step's sort
   layout_dirty_ = scenes_dirty_ = true;
   carry_valid_ = false;
+  bool any_live = false;
+  for (uint32_t s = 0; s < max_scenes_ && !any_live; ++s) any_live = scenes_[s].live;
+  if (any_live) {
+    free_.emplace_back(old_base_[id], scenes_[id].n);  // reusable before then
+  } else {
+    free_.clear();  // nothing left to keep: the layout starts over
+    layout_total_ = 0;
+  }
   return SPH_OK;
 }
 
@@ -551,6 +574,7 @@ int Engine::Step(int substeps, cudaStream_t st) {
       if (scenes_[s].live) old_base_[s] = scenes_[s].base;
     layout_total_ = total_;
     layout_dirty_ = false;
+    free_.clear();
     for (auto& sc : scenes_)
       if (sc.used && !sc.live) sc.used = false;
   }

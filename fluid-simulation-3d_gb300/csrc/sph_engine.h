@@ -85,6 +85,11 @@ class Engine {
   std::vector<Scene> scenes_;
   std::vector<uint32_t> old_base_;  // per scene: base in the layout a step reads
   uint64_t layout_total_ = 0;       // slots occupied in the current layout
+  // Free extents (base, length) of the current layout: the regions of scenes
+  // removed since the last step compacted it. AddScene loads a new scene into
+  // the first one that fits before it appends past the layout's end, so the
+  // room a removed scene leaves is usable before the next step.
+  std::vector<std::pair<uint64_t, uint64_t>> free_;
   uint32_t total_ = 0;              // live particles (table length)
   bool layout_dirty_ = true;
   bool scenes_dirty_ = true;

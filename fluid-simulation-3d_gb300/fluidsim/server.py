@@ -7,9 +7,12 @@ allowed to backfill. A request is admitted while the HBM state budget
 room. Admitted state stays resident on the device, and every resident scene
 advances one step per batched launch, so requests that arrive while others
 run share the device with them. A request leaves, with its final state read
-back, after its K-th step. The loop records each request's per-step
-latency: the wall time of the batched step it took part in, measured with a
-stream sync around the step.
+back, after its K-th step. A request can be withdrawn with cancel() (for
+instance from the per-step callback): it is dropped if it has not been
+admitted, and a resident one leaves the batch at the next step boundary,
+freeing its capacity for the requests still waiting. The loop records each
+request's per-step latency: the wall time of the batched step it took part
+in, measured with a stream sync around the step.
 
 The batched step runs the same per-particle arithmetic in the same order as a
 scene stepped alone, so every result is the same alone and in the mix (the
@@ -67,9 +70,28 @@ class Server:
         if tuning:
             self.batch.set_tuning(**tuning)
         self.resident = {}  # scene id -> [request, steps left, admitted, step_ms]
+        self._cancel = set()  # request ids to withdraw at the next boundary
 
     def close(self):
         self.batch.close()
+
+    def cancel(self, rid: int) -> None:
+        """Withdraw request `rid` at the next step boundary of run(); it
+        returns no result. Ids of requests already finished are ignored."""
+        self._cancel.add(int(rid))
+
+    def _apply_cancels(self, pending, waiting, cancelled):
+        if not self._cancel:
+            return
+        for queue in (pending, waiting):
+            for req in [r for r in queue if r.rid in self._cancel]:
+                queue.remove(req)
+                cancelled.append(req.rid)
+        for sid in [s for s, v in self.resident.items() if v[0].rid in self._cancel]:
+            req = self.resident.pop(sid)[0]
+            self.batch.remove(sid)
+            cancelled.append(req.rid)
+        self._cancel.clear()
 
     def _admit(self, waiting, now):
         admitted = []
@@ -91,12 +113,13 @@ class Server:
         if len(substeps) > 1:
             raise ValueError("one substep count per server")
         substeps = substeps.pop() if substeps else 1
-        waiting, done = [], {}
+        waiting, done, cancelled = [], {}, []
         t0 = time.perf_counter()
         offset = 0.0  # time skipped while idle (realtime=False)
         lat, steps, pstep = [], 0, 0
         peak_resident = 0
         while pending or waiting or self.resident:
+            self._apply_cancels(pending, waiting, cancelled)
             now = time.perf_counter() - t0 + offset
             while pending and pending[0].arrival <= now:
                 waiting.append(pending.pop(0))
@@ -138,7 +161,8 @@ class Server:
         wall = time.perf_counter() - t0
         lat = np.asarray(lat) if lat else np.zeros(1)
         stats = dict(
-            requests=len(done), batched_steps=steps, particle_steps=int(pstep),
+            requests=len(done), cancelled=sorted(cancelled),
+            batched_steps=steps, particle_steps=int(pstep),
             wall_s=wall, particle_steps_per_s=pstep / max(wall, 1e-9),
             p50_step_ms=float(np.percentile(lat, 50)),
             p99_step_ms=float(np.percentile(lat, 99)),

@@ -30,7 +30,8 @@ extern "C" {
 #define SPH_ERR_CUDA -2      /* CUDA runtime error / no device            */
 #define SPH_ERR_NOMEM -3     /* device allocation or budget exhausted     */
 #define SPH_ERR_STATE -4     /* call not valid in the handle's state      */
-#define SPH_ERR_DEVICE -5    /* a kernel raised a device status flag      */
+#define SPH_ERR_DEVICE -5    /* reserved: no call returns it; kernel
+                                status flags are read with sph_status     */
 
 /* Device status flags (sph_status). */
 #define SPH_STATUS_NONFINITE 0x1u  /* a position/velocity became NaN/inf   */

@@ -107,3 +107,83 @@ def test_served_results_match_alone(gpu_lib):
         for g, e in zip((done[r.rid].pos, done[r.rid].vel, done[r.rid].dens), ref):
             assert np.array_equal(g, e), r.rid
     assert stats["p99_step_ms"] >= stats["p50_step_ms"] > 0
+
+
+def served_requests(count, seed, steps, lo=2100, hi=2900):
+    from fluidsim import scenes, server
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(count):
+        sc = scenes.request_scene(rng, lo=lo, hi=hi, kmin=3, kmax=3)
+        reqs.append(server.Request(k, sc["params"], sc["pos"], sc["vel"], sc["dt"],
+                                   sc["substeps"], steps[k], arrival=0.0))
+    return reqs
+
+
+def test_served_cancellation_frees_capacity(gpu_lib):
+    """A budget of two requests at a time: cancelling a long resident request
+    admits a waiting one in its place, a cancelled waiting request never
+    runs, and every finished request still equals its run alone."""
+    from fluidsim import server
+    reqs = served_requests(4, seed=31, steps=[40, 3, 3, 3])
+    srv = server.Server(2 * 2900 * server.bytes_per_particle(), max_scenes=8)
+
+    def on_step(step, ms, resident):
+        if step == 2:
+            srv.cancel(0)  # resident, 38 steps left
+            srv.cancel(3)  # still waiting for room
+
+    done, stats = srv.run(reqs, realtime=False, on_step=on_step)
+    srv.close()
+    assert stats["cancelled"] == [0, 3]
+    assert sorted(done) == [1, 2]
+    # request 2 only fits once request 0 has left: it runs steps 3..5
+    assert stats["batched_steps"] == 5
+    for rid in (1, 2):
+        ref = server.run_alone(reqs[rid])
+        for g, e in zip((done[rid].pos, done[rid].vel, done[rid].dens), ref):
+            assert np.array_equal(g, e), rid
+
+
+def test_served_request_beyond_budget_is_refused(gpu_lib):
+    from fluidsim import server
+    reqs = served_requests(1, seed=32, steps=[2])
+    srv = server.Server(1000 * server.bytes_per_particle(), max_scenes=4)
+    with pytest.raises(RuntimeError, match="exceeds the capacity"):
+        srv.run(reqs, realtime=False)
+    srv.close()
+
+
+def test_removed_scene_room_is_reused_before_the_next_step(gpu_lib):
+    """A scene added right after another was removed takes over its room in
+    the current layout (no step in between needed); with every scene
+    removed the whole capacity is free again. Results equal each scene run
+    alone."""
+    import fluidsim
+    scs = sorted(small_scenes(3, seed=13), key=lambda s: -s["pos"].shape[0])
+    big, mid, small = scs
+    n = [s["pos"].shape[0] for s in scs]
+    assert n[2] < n[0]
+    b = fluidsim.Batch(n[0] + n[1], 8)
+    a = b.add(big["params"], big["pos"], big["vel"], big["dt"])
+    m = b.add(mid["params"], mid["pos"], mid["vel"], mid["dt"])
+    b.step(3)
+    b.remove(a)
+    s = b.try_add(small["params"], small["pos"], small["vel"], small["dt"])
+    assert s is not None
+    # what is left of the big scene's room and the layout's end is too small
+    assert b.try_add(big["params"], big["pos"], big["vel"], big["dt"]) is None
+    b.step(3); b.step(3)
+    for sid, sc, k in ((m, mid, 3), (s, small, 2)):
+        got = b.download(sid)
+        for g, r in zip(got, alone(sc, k)):
+            assert np.array_equal(g, r), sid
+    b.remove(m)
+    b.remove(s)
+    a2 = b.add(big["params"], big["pos"], big["vel"], big["dt"])
+    m2 = b.add(mid["params"], mid["pos"], mid["vel"], mid["dt"])
+    b.step(3)
+    for sid, sc in ((a2, big), (m2, mid)):
+        for g, r in zip(b.download(sid), alone(sc, 1)):
+            assert np.array_equal(g, r), sid
+    b.close()
