@@ -738,6 +738,28 @@ int Engine::SetTuning(const sph_tuning& t) {
 int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
                      float* best_ms, cudaStream_t st) {
   if (steps_per_trial < 1) return Fail(SPH_ERR_INVALID, "steps_per_trial >= 1");
+  // The sweep times real steps. Every live scene's state (positions,
+  // velocities, densities and OutPositions, in caller order) is kept on the
+  // host meanwhile and loaded back afterwards, so tuning leaves the
+  // simulation where it was.
+  struct Saved {
+    uint32_t id;
+    std::vector<float> pos, vel, dens;
+    std::vector<float4> out;
+  };
+  std::vector<Saved> saved;
+  for (uint32_t s = 0; s < max_scenes_; ++s) {
+    if (!scenes_[s].live) continue;
+    const uint32_t n = scenes_[s].n;
+    Saved v{s, std::vector<float>(3 * size_t{n}), std::vector<float>(3 * size_t{n}),
+            std::vector<float>(2 * size_t{n}), std::vector<float4>(n)};
+    const int r = Download(s, v.pos.data(), v.vel.data(), v.dens.data(), false, st);
+    if (r != SPH_OK) return r;
+    SPH_CUDA(cudaMemcpyAsync(v.out.data(), d_out4_ + old_base_[s], sizeof(float4) * n,
+                             cudaMemcpyDeviceToHost, st), "save OutPositions");
+    saved.push_back(std::move(v));
+  }
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   sph_tuning win = tuning_;
   float win_ms = std::numeric_limits<float>::infinity();
   cudaEvent_t e0, e1;
@@ -773,6 +795,20 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  for (const Saved& v : saved) {
+    // Load puts the scene back in caller order at its current base, where
+    // the saved densities and OutPositions line up slot for slot.
+    const int r = Load(v.id, v.pos.data(), v.vel.data(), false, st);
+    if (r == SPH_OK) {
+      const uint32_t n = scenes_[v.id].n, b = old_base_[v.id];
+      SPH_CUDA(cudaMemcpyAsync(ctx_.dens_a + b, v.dens.data(), sizeof(float2) * n,
+                               cudaMemcpyHostToDevice, st), "restore densities");
+      SPH_CUDA(cudaMemcpyAsync(d_out4_ + b, v.out.data(), sizeof(float4) * n,
+                               cudaMemcpyHostToDevice, st), "restore OutPositions");
+    }
+    if (rc == SPH_OK) rc = r;
+  }
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");  // host copies die here
   if (rc != SPH_OK) return rc;
   rc = SetTuning(win);
   if (best) *best = win;

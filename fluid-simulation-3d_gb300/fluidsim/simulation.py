@@ -217,8 +217,9 @@ class FluidSimulation:
                     force_block=t.force_block)
 
     def autotune(self, deltatime, substeps=1, steps_per_trial=2):
-        """Sweep the launch configuration on real steps (the state advances);
-        keeps the fastest. Returns (tuning dict, ms per step)."""
+        """Sweep the launch configuration on real steps and keep the fastest;
+        the state is saved before the sweep and restored after it. Returns
+        (tuning dict, ms per step)."""
         t = Tuning()
         ms = ctypes.c_float()
         check(self._lib.sph_autotune(self._h, _f32(deltatime), int(substeps),
@@ -419,6 +420,9 @@ class Batch:
                     force_block=t.force_block)
 
     def autotune(self, substeps: int, steps_per_trial: int = 2):
+        """Sweep the launch configuration on real steps of the resident
+        scenes and keep the fastest; every scene's state is saved before the
+        sweep and restored after it. Returns (tuning dict, ms per step)."""
         t = Tuning()
         ms = ctypes.c_float()
         self._check(self._lib.sph_batch_autotune(self._h, int(substeps), int(steps_per_trial),

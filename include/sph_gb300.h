@@ -63,9 +63,10 @@ typedef struct sph_sim sph_sim;
 typedef struct sph_tuning {
   int32_t block;      /* threads per block of the neighbour kernels
                          (multiple of 32, 32..1024), default 128          */
-  int32_t cell_tile;  /* candidates of a cell held in a warp's registers
-                         per pass of the density kernel: 64, 128, 192 or
-                         256 (default 128)                                */
+  int32_t cell_tile;  /* density kernel: 1 = one lane per particle walking
+                         its cell's runs (default); 64, 128, 192 or 256 =
+                         warp-cooperative form holding that many candidates
+                         of a cell in registers per pass                  */
   int32_t particles_per_warp; /* particles per warp: 32 (one per lane)    */
   int32_t gather;     /* neighbour-list entries whose gathers the force
                          kernels issue together: 2, 4 or 8 (default 4)    */
@@ -153,9 +154,12 @@ int sph_profile_enable(sph_sim *sim, int enable);
 int sph_phase_times(sph_sim *sim, double out_ms[6]);
 
 /* Kernel launch configuration of a single-scene handle, and its autotuner:
- * sweeps block size and gather batch on real steps of dt/substeps (the state
- * advances by steps_per_trial + 1 steps per candidate), keeps the fastest
- * and reports it (best may be NULL) with its ms per step. */
+ * times real steps of dt/substeps (steps_per_trial per candidate, after one
+ * untimed step) over the neighbour block size x cell tile, then the force
+ * kernels' block size, then the gather batch; keeps the fastest and reports
+ * it (best may be NULL) with its ms per step. The state (positions,
+ * velocities, densities, OutPositions) is saved before the sweep and
+ * restored after it. */
 int sph_set_tuning(sph_sim *sim, const sph_tuning *t);
 int sph_get_tuning(const sph_sim *sim, sph_tuning *t);
 int sph_autotune(sph_sim *sim, float dt, int substeps, int steps_per_trial,
@@ -242,9 +246,10 @@ int sph_batch_download(sph_batch *b, uint32_t scene_id, float *pos3,
  * (see sph_tuning above). */
 int sph_batch_set_tuning(sph_batch *b, const sph_tuning *t);
 int sph_batch_get_tuning(const sph_batch *b, sph_tuning *t);
-/* Sweep the tuning space on the resident scenes (runs real steps, so the
- * state advances by `steps_per_trial` steps per candidate), keep the fastest
- * and report it in *best (may be NULL) and its ms per step in *best_ms. */
+/* Sweep the tuning space on the resident scenes as sph_autotune does (real
+ * steps; every scene's state is saved before and restored after), keep the
+ * fastest and report it in *best (may be NULL) and its ms per step in
+ * *best_ms. */
 int sph_batch_autotune(sph_batch *b, int substeps, int steps_per_trial,
                        sph_tuning *best, float *best_ms, void *stream);
 

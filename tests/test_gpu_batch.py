@@ -77,14 +77,50 @@ def test_batch_autotune(gpu_lib):
     import fluidsim
     scs = small_scenes(4, seed=11)
     b = fluidsim.Batch(sum(s["pos"].shape[0] for s in scs), 8)
-    for s in scs:
-        b.add(s["params"], s["pos"], s["vel"], s["dt"])
+    ids = [b.add(s["params"], s["pos"], s["vel"], s["dt"]) for s in scs]
+    b.step(3)
+    before = [b.download(i) for i in ids]
     best, ms = b.autotune(3, steps_per_trial=1)
     assert best["block"] in (64, 128, 256, 512)
     assert best["cell_tile"] in (1, 64, 128, 256)
+    assert best["force_block"] in (64, 128, 256, 512)
+    assert best["gather"] in (2, 4, 8)
     assert ms > 0.0
     assert b.tuning() == best
+    # the sweep's trial steps leave no trace in the scenes' state
+    for i, was in zip(ids, before):
+        for g, e in zip(b.download(i), was):
+            assert np.array_equal(g, e), i
     b.close()
+
+
+def out_positions(sim, n):
+    import ctypes
+    host = np.empty((n, 4), np.float32)
+    rt = ctypes.CDLL("libcudart.so.13")  # the runtime the library loaded
+    rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                              ctypes.c_int]
+    assert rt.cudaMemcpy(host.ctypes.data, sim.out_positions_device_ptr(), n * 16, 2) == 0
+    return host
+
+
+def test_single_scene_autotune_restores_state(gpu_lib):
+    import fluidsim
+    sc = small_scenes(1, seed=12, lo=3000, hi=4000)[0]
+    n = sc["pos"].shape[0]
+    sim = fluidsim.FluidSimulation(sc["params"])
+    sim.InitializeData(n, sc["pos"], sc["vel"])
+    sim.Update(sc["dt"], 3)
+    before = sim.download()
+    out_before = out_positions(sim, n)
+    best, ms = sim.autotune(sc["dt"], 3, steps_per_trial=1)
+    assert ms > 0.0 and sim.tuning() == best
+    for g, e in zip(sim.download(), before):
+        assert np.array_equal(g, e)
+    assert np.array_equal(out_positions(sim, n), out_before)
+    sim.Update(sc["dt"], 3)  # and it steps on from there
+    assert sim.status() == 0
+    sim.close()
 
 
 def test_served_results_match_alone(gpu_lib):
