@@ -3,12 +3,29 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <limits>
 
 namespace sph {
 
 namespace {
+
+// The device address of a host array the device can reach directly (pinned
+// memory mapped into its address space) when 16-byte aligned; nullptr for
+// pageable memory, other alignments and nullptr. (Downloads keep the copy
+// engine: SM stores over the host link measured slower than its copies.)
+template <class T> T* DeviceAlias(T* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();  // not an error for the caller: use the staged copy
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  if (reinterpret_cast<std::uintptr_t>(a.devicePointer) & 15u) return nullptr;
+  return static_cast<T*>(a.devicePointer);
+}
 
 constexpr float kPiF = 3.14159265358979323846f;  // glm::pi<float>()
 
@@ -325,7 +342,13 @@ int Engine::Load(uint32_t id, const float* pos3, const float* vel3,
   carry_valid_ = false;  // a new state needs its own prediction
   const float* dp = pos3;
   const float* dv = vel3;
-  if (!device_ptrs && pos3) {
+  const float* hp = device_ptrs ? nullptr : DeviceAlias(pos3);
+  const float* hv = device_ptrs ? nullptr : DeviceAlias(vel3);
+  if (hp && (!vel3 || hv)) {
+    // pinned host rows: the import kernel reads them over the link itself
+    SPH_CUDA(launch_import_rows(old_base_[id], n, hp, hv, d_pos_[cur_], d_vel_[cur_], st),
+             "import kernel");
+  } else if (!device_ptrs && pos3) {
     // Stage through the prediction / post-pressure buffers (rewritten by
     // every substep before use).
     float* sp = reinterpret_cast<float*>(ctx_.pred);
@@ -340,8 +363,9 @@ int Engine::Load(uint32_t id, const float* pos3, const float* vel3,
   } else if (!pos3) {
     dv = nullptr;
   }
-  SPH_CUDA(launch_import(old_base_[id], n, dp, dv, d_pos_[cur_], d_vel_[cur_], st),
-           "import kernel");
+  if (!(hp && (!vel3 || hv)))
+    SPH_CUDA(launch_import(old_base_[id], n, dp, dv, d_pos_[cur_], d_vel_[cur_], st),
+             "import kernel");
   // Densities are unknown until the next step.
   SPH_CUDA(cudaMemsetAsync(ctx_.dens_a + old_base_[id], 0, sizeof(float2) * n, st),
            "cudaMemsetAsync");

@@ -1010,6 +1010,52 @@ __global__ void k_import(uint32_t first, uint32_t n,
                         : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// Upload straight from host memory (pinned buffers the device can address,
+// read over the CPU link): the caller-order float3 rows of 32 consecutive
+// particles are 384 contiguous bytes, 24 float4. Each warp reads its chunk as
+// aligned float4 (the link's transactions stay full) and transposes it
+// through shared memory; a partial last chunk goes by scalar loads, so
+// nothing outside the 3n floats is touched. The arrays must be 16-byte
+// aligned (checked by the launcher's caller).
+constexpr int kXferBlock = 256;
+constexpr int kXferWarps = kXferBlock / 32;
+
+__global__ void __launch_bounds__(kXferBlock)
+k_import_rows(uint32_t first, uint32_t n, const float* __restrict__ ipos,
+              const float* __restrict__ ivel, float4* __restrict__ pos,
+              float4* __restrict__ vel) {
+  __shared__ __align__(16) float s_rows[kXferWarps][2][96];
+  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+  const uint32_t k0 = (blockIdx.x * kXferWarps + w) * 32u;
+  if (k0 >= n) return;  // whole warp
+  const uint32_t cnt = min(32u, n - k0);
+  float* sp = s_rows[w][0];
+  float* sv = s_rows[w][1];
+  const uint64_t f0 = 3ull * k0;
+  if (cnt == 32u) {
+    if (lane < 24u) {
+      reinterpret_cast<float4*>(sp)[lane] =
+          __ldcs(reinterpret_cast<const float4*>(ipos + f0) + lane);
+      if (ivel)
+        reinterpret_cast<float4*>(sv)[lane] =
+            __ldcs(reinterpret_cast<const float4*>(ivel + f0) + lane);
+    }
+  } else {
+    for (uint32_t e = lane; e < 3u * cnt; e += 32u) {
+      sp[e] = ipos[f0 + e];
+      if (ivel) sv[e] = ivel[f0 + e];
+    }
+  }
+  __syncwarp();
+  if (lane < cnt) {
+    const uint32_t k = k0 + lane;
+    pos[first + k] = make_float4(sp[3 * lane], sp[3 * lane + 1], sp[3 * lane + 2],
+                                 __uint_as_float(k));
+    vel[first + k] = ivel ? make_float4(sv[3 * lane], sv[3 * lane + 1], sv[3 * lane + 2], 0.0f)
+                          : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------- launchers
@@ -1175,6 +1221,16 @@ cudaError_t launch_import(uint32_t first, uint32_t n, const float* ipos,
                           cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   k_import<<<(n + 255) / 256, 256, 0, st>>>(first, n, ipos, ivel, pos, vel);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_import_rows(uint32_t first, uint32_t n, const float* ipos,
+                               const float* ivel, float4* pos, float4* vel,
+                               cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const uint32_t warps = (n + 31) / 32;
+  k_import_rows<<<(warps + kXferWarps - 1) / kXferWarps, kXferBlock, 0, st>>>(
+      first, n, ipos, ivel, pos, vel);
   return cudaGetLastError();
 }
 

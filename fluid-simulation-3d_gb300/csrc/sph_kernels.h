@@ -129,5 +129,10 @@ cudaError_t launch_ref_lookup(const LaunchCtx& c, const Tiles& new_tiles,
 cudaError_t launch_import(uint32_t first, uint32_t n, const float* ipos,
                           const float* ivel, float4* pos, float4* vel,
                           cudaStream_t st);
+// The same import reading host memory the device addresses directly (pinned
+// buffers, 16-byte aligned): rows move as aligned float4 per warp.
+cudaError_t launch_import_rows(uint32_t first, uint32_t n, const float* ipos,
+                               const float* ivel, float4* pos, float4* vel,
+                               cudaStream_t st);
 
 }  // namespace sph

@@ -5,7 +5,9 @@
  * (engine/physics/physicsWorld.cc): spatial-hash build, density and near
  * density, pressure + near pressure + viscosity, integrate with box
  * collision. The library owns all device memory; host pointers passed in are
- * caller-owned and only read/written during the call. Every call returns an
+ * caller-owned and only read/written during the call -- except page-locked
+ * (pinned) input arrays, which the upload calls read asynchronously on the
+ * stream, as cudaMemcpyAsync does (see sph_upload). Every call returns an
  * int status (SPH_OK = 0); sph_last_error() gives the message of the last
  * failure on a handle. A handle is used from one host thread and enqueues its
  * work on the caller's CUDA stream (passed as a plain pointer, NULL = the
@@ -92,7 +94,12 @@ int sph_get_params(const sph_sim *sim, sph_params *out);
 uint32_t sph_num_particles(const sph_sim *sim);
 
 /* Load positions / velocities (host, float[3n]; vel may be NULL = zero).
- * Replaces writing the public `positions` buffer (physicsWorld.h:79). */
+ * Replaces writing the public `positions` buffer (physicsWorld.h:79).
+ * Pageable arrays are copied before the call returns. Page-locked arrays
+ * (cudaHostAlloc, or registered) are read when `stream` reaches the call --
+ * 16-byte aligned ones by the import kernel itself, over the host link --
+ * so keep them unchanged until then (a later sph_download on the same
+ * stream has passed it). */
 int sph_upload(sph_sim *sim, const float *pos3, const float *vel3,
                void *stream);
 
