@@ -44,7 +44,8 @@ UNIT = "particle-steps/s"
 # writes of its inputs and outputs once), for the roofline.
 ALG_BYTES = {
     "predict_hash": 44,   # pos 16 + vel 16 in; key/rank 8 + count 4 out
-    "spatial": 132,       # scan 12 + scatter 24 + reorder 96
+    "spatial": 172,       # scan 12 + scatter 24 + reorder 96 + cell table ~40
+                          # (216 B of row runs per cell, ~5.4 particles a cell)
     "density": 44,        # pred 16 + start 4 in; dens_a 8 + dens_b 16 out
     "pressure": 76,       # pred 16, start 4, dens_a 8, dens_b 16, vel 16 in; velp 16 out
     "viscosity": 84,      # pred 16, start 4, velp 16, pos 16 in; pos 16 + vel 16 out
@@ -411,6 +412,19 @@ def run_native(args):
     peak, peak_kind = peaks()
     achieved = ALG_BYTES[dom] * n / (per_launch_ms[dom] / 1000.0) / 1e9
     tr = ncu_traffic(args.workload, dom)
+    # every phase against the same peak: the sort (scan, scatter, reorder,
+    # cell table), density and the two force kernels; the prediction is
+    # fused into the viscosity kernel while it is carried between steps
+    phase_roofline = {}
+    for nm in ["spatial", "density", "pressure", "viscosity"]:
+        ach = ALG_BYTES[nm] * n / (per_launch_ms[nm] / 1000.0) / 1e9
+        parts = {"spatial": ["reorder", "cell_table"]}.get(nm, [nm])
+        tp = [ncu_traffic(args.workload, k) for k in parts]
+        phase_roofline[nm] = {
+            "ms_per_launch": per_launch_ms[nm], "alg_bytes_per_particle": ALG_BYTES[nm],
+            "achieved_GBps": ach, "frac": ach / peak,
+            "dram_bytes_per_particle": (sum(tp) if all(x is not None for x in tp) else None),
+            "dram_bytes_of": "+".join(parts)}
     ms_step = total_ms / args.steps
     sub_ms = ms_step / S
     line = {
@@ -436,7 +450,8 @@ def run_native(args):
         "substep": {"ms": sub_ms,
                     "alg_GBps_at_300B": SURVEY_BYTES_PER_SUBSTEP * n / (sub_ms / 1000) / 1e9,
                     "frac_at_300B": SURVEY_BYTES_PER_SUBSTEP * n / (sub_ms / 1000) / 1e9 / peak,
-                    "phase_ms_per_launch": per_launch_ms, "phase_share": share},
+                    "phase_ms_per_launch": per_launch_ms, "phase_share": share,
+                    "phase_roofline": phase_roofline},
         "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
                 "warmup": args.warmup,
                 "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n},
