@@ -117,7 +117,8 @@ __device__ __forceinline__ uint32_t cell_index(const SceneDev& S, float3 pr) {
 }
 
 // Run-length flag of a cell-table row whose three x-runs are one contiguous
-// run (stored in the row's first entry; the other two entries are empty).
+// run (stored in the row's first entry; the other two entries of such a row
+// are not written and must not be read).
 constexpr uint32_t kRunMerged = 0x80000000u;
 
 }  // namespace sph

@@ -402,7 +402,9 @@ __device__ __forceinline__ uint2 bucket_run(uint32_t cell, uint32_t b0,
 // rows (dy, dz) of three x-runs. The x-neighbours of a row have consecutive
 // cell indices, hence consecutive keys; when their runs are adjacent in the
 // layout (their buckets hold no other cell -- the usual case inside the box)
-// the row is stored as one run flagged kRunMerged. Lanes take (cell, row)
+// the row is stored as one run flagged kRunMerged in its first entry (its
+// other two entries are left unwritten: a third of the table's stores, which
+// the readers skip). Lanes take (cell, row)
 // pairs of the warp's tile in parallel; the warp's cell leaders are listed
 // in shared memory (kCellTableBlock threads per block).
 constexpr int kCellTableBlock = 256;
@@ -466,8 +468,6 @@ k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
       uint2* out = cell_tab + static_cast<uint64_t>(slot) * 27u + 3u * w;
       if (adjacent) {
         out[0] = make_uint2(f, (e - f) | kRunMerged);
-        out[1] = make_uint2(e, 0u);
-        out[2] = make_uint2(e, 0u);
       } else {
         out[0] = run[0];
         out[1] = run[1];
@@ -601,6 +601,10 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
       const uint32_t cfc = __shfl_sync(kFull, cf, c0);
       uint2 run = make_uint2(0u, 0u);
       if (lane < 27) run = __ldg(cell_tab + static_cast<uint64_t>(cfc) * 27u + lane);
+      // a merged row keeps its run in its first entry; the other two are unused
+      const uint32_t heads =
+          __ballot_sync(kFull, lane < 27u && lane % 3u == 0u && (run.y & kRunMerged));
+      if (lane < 27u && lane % 3u != 0u && ((heads >> (lane - lane % 3u)) & 1u)) run.y = 0u;
       run.y &= ~kRunMerged;
       const uint32_t incl = warp_incl_scan(run.y);
       const uint32_t excl = incl - run.y;

@@ -11,11 +11,13 @@ from parity import compare_substep
 pytestmark = pytest.mark.gpu
 
 
-def run_substep(fx, params, debug=True):
+def run_substep(fx, params, debug=True, tuning=None):
     import fluidsim
     sim = fluidsim.FluidSimulation(params)
     n = fx["pos_in"].shape[0]
     sim.InitializeData(n, fx["pos_in"], fx["vel_in"])
+    if tuning:
+        sim.set_tuning(**tuning)
     if debug:
         sim.debug_enable(True)
     sim.Update(float(fx["dt"]), 1)
@@ -35,6 +37,23 @@ def test_substep_parity(gpu_lib, name):
     assert np.array_equal(got["dens"], dens)
     rep = compare_substep(got, fx, float(fx["dt"]), pos, vel)
     print(name, rep)
+
+
+@pytest.mark.parametrize("tile", [64, 128, 192, 256])
+@pytest.mark.parametrize("name", ["substep_dam_break_16k.npz", "substep_wrapped_grid.npz",
+                                  "substep_single_cell.npz", "substep_n1000_cloud.npz",
+                                  "substep_coincident.npz"])
+def test_substep_parity_cooperative_density(gpu_lib, name, tile):
+    """The autotuner's other density form (a warp per cell, candidates of
+    the cell's runs held in registers, `tile` at a time) under the same
+    contract."""
+    fx = load_fixture(name)
+    p = fixture_params(fx)
+    fx["bound"] = np.array(p.bound, np.float64)
+    got, pos, vel, dens = run_substep(fx, p, tuning=dict(cell_tile=tile))
+    assert np.array_equal(got["dens"], dens)
+    rep = compare_substep(got, fx, float(fx["dt"]), pos, vel)
+    print(name, tile, rep)
 
 
 def test_large_scene_parity(gpu_lib):
