@@ -202,7 +202,7 @@ __global__ void k_predict_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
 }
 
 // -------------------------------------------------------------------- scan
-constexpr int kScanThreads = 1024;
+constexpr int kScanThreads = 512;
 constexpr int kScanItems = 4;
 constexpr int kScanBlock = kScanThreads * kScanItems;
 constexpr uint32_t kScanFoldBlocks = 4096;  // fold the partials scan up to here
