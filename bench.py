@@ -475,7 +475,7 @@ def run_native(args):
     except Exception as e:  # scipy missing: leave the block out
         print(f"pair statistics skipped: {e}", file=sys.stderr)
     if not args.no_cpu_baseline and world == 1:
-        rate, steps, el, th = cpu_port_rate(sc, max_steps=4, budget_s=8.0)
+        rate, steps, el, th = cpu_port_rate(sc, max_steps=16, budget_s=12.0)  # ~10-15 s
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": th, "kind": "port",
             "sample": f"{steps} full steps of the {n}-particle scene "
