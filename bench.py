@@ -21,6 +21,7 @@ own build where it exists here) on the same workload.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import pathlib
@@ -256,6 +257,47 @@ def cpu_port_rate(sc, max_steps, budget_s, threads=0):
     return n * steps / el, steps, el, th
 
 
+def time_render(sim, sc, stream, warmup, width=1920, height=1080, frames=10):
+    """Headless render (sph_render) of the scene's last state at 1080p from a
+    camera that sees the whole box: device ms per frame (splat + resolve,
+    CUDA events on the library's stream) and ms per frame with the RGBA8 and
+    depth images read back to host memory."""
+    import torch
+
+    from fluidsim import render
+    hx, hy, hz = (0.5 * b for b in sc["params"].bound)
+    v = render.view((0.9 * hx, 1.1 * hy, 1.9 * hz), (-0.2 * hx, -0.6 * hy, -0.2 * hz),
+                    width, height)
+    lib, h, st = sim._lib, sim.handle, sim._stream
+    vref = ctypes.byref(v)
+    for _ in range(max(warmup, 1)):
+        if lib.sph_render(h, vref, None, None, st) != 0:
+            raise RuntimeError("render failed")
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(frames):
+        lib.sph_render(h, vref, None, None, st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dev_ms = e0.elapsed_time(e1) / frames
+    rgba = torch.empty((height, width, 4), dtype=torch.uint8, pin_memory=True).numpy()
+    depth = torch.empty((height, width), dtype=torch.float32, pin_memory=True).numpy()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        lib.sph_render(h, vref, rgba.ctypes.data, depth.ctypes.data, st)
+    host_ms = (time.perf_counter() - t0) * 1000.0 / frames
+    n = sc["pos"].shape[0]
+    return {"width": width, "height": height, "particles": n,
+            "ms_per_frame": dev_ms, "frames_per_s": 1000.0 / dev_ms,
+            "ms_per_frame_with_readback": host_ms,
+            "covered_frac": float((depth < 1.0).mean()),
+            "readback_bytes": 8 * width * height,
+            "timing": "device: CUDA events around the frames on the library's stream; "
+                      "with readback: wall clock, RGBA8 + depth copied to pinned memory"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -393,6 +435,7 @@ def run_native(args):
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, "cuda")
     e2e_value = world * n * e2e_steps / e2e_s
+    render_block = time_render(sim, sc, stream, args.warmup)
     sim_tuning = sim.tuning()
     sim.close()
 
@@ -456,6 +499,7 @@ def run_native(args):
                 "warmup": args.warmup,
                 "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n},
         "wall_s": wall,
+        "render": render_block,
     }
     if clk:
         line["clocks"] = clk

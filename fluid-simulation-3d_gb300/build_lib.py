@@ -16,7 +16,8 @@ PKG = pathlib.Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libsph_gb300.so"
-SOURCES = ["sph_kernels.cu", "sph_engine.cu", "sph_capi.cu", "sph_static.cu"]
+SOURCES = ["sph_kernels.cu", "sph_engine.cu", "sph_capi.cu", "sph_static.cu",
+           "sph_render.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -131,6 +131,12 @@ int sph_download_device(sph_sim* sim, float* dpos3, float* dvel3, float* ddens2,
   return sim->eng.Download(sim->scene, dpos3, dvel3, ddens2, true, S(stream));
 }
 
+int sph_render(sph_sim* sim, const sph_view* view, uint8_t* rgba, float* depth,
+               void* stream) {
+  if (!sim || !view) return SPH_ERR_INVALID;
+  return sim->eng.Render(sim->scene, *view, rgba, depth, S(stream));
+}
+
 int sph_out_positions(sph_sim* sim, void** dev_float4) {
   if (!sim) return SPH_ERR_INVALID;
   return sim->eng.OutPositions(sim->scene, dev_float4);
@@ -239,6 +245,12 @@ int sph_batch_download(sph_batch* b, uint32_t scene_id, float* pos3,
                        float* vel3, float* dens2, void* stream) {
   if (!b) return SPH_ERR_INVALID;
   return b->eng.Download(scene_id, pos3, vel3, dens2, false, S(stream));
+}
+
+int sph_batch_render(sph_batch* b, uint32_t scene_id, const sph_view* view,
+                     uint8_t* rgba, float* depth, void* stream) {
+  if (!b || !view) return SPH_ERR_INVALID;
+  return b->eng.Render(scene_id, *view, rgba, depth, S(stream));
 }
 
 int sph_batch_set_tuning(sph_batch* b, const sph_tuning* t) {

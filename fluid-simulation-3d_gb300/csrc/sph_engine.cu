@@ -1,5 +1,6 @@
 // Host engine of the SPH substep pipeline (see sph_engine.h).
 #include "sph_engine.h"
+#include "sph_render.h"
 
 #include <algorithm>
 #include <cmath>
@@ -130,7 +131,8 @@ Engine::~Engine() {
                   ctx_.partial, d_out4_, d_status_, d_dbg_hash_, d_dbg_key_,
                   d_dbg_accp_, d_dbg_velv_, d_dbg_velp_, d_dbg_start_,
                   d_dbg_count_, d_dbg_partial_, d_dbg_keyrank_, d_dbg_tmp_,
-                  d_dbg_sorted_, d_dbg_scratch_};
+                  d_dbg_sorted_, d_dbg_scratch_, d_rkeys_, d_rrgba_, d_rdepth_,
+                  d_rcolour_};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -636,6 +638,68 @@ int Engine::Download(uint32_t id, float* pos3, float* vel3, float* dens2,
       SPH_CUDA(cudaMemcpyAsync(dens2, scratch_d, sizeof(float) * 2 * n,
                                cudaMemcpyDeviceToHost, st), "download densities");
   }
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  return SPH_OK;
+}
+
+int Engine::Render(uint32_t id, const sph_view& v, uint8_t* rgba, float* depth,
+                   cudaStream_t st) {
+  if (id >= max_scenes_ || !scenes_[id].live)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  const uint64_t pixels = static_cast<uint64_t>(v.width) * v.height;
+  if (v.width == 0 || v.height == 0 || pixels > (1ull << 28))
+    return Fail(SPH_ERR_INVALID, "image size must be in [1, 2^28] pixels");
+  const float* P = v.proj;
+  if (!(P[0] > 0.0f) || !(P[5] > 0.0f) || P[1] != 0.0f || P[2] != 0.0f || P[3] != 0.0f ||
+      P[4] != 0.0f || P[6] != 0.0f || P[7] != 0.0f)
+    return Fail(SPH_ERR_INVALID,
+                "projection columns 0 and 1 must be (a,0,0,0) and (0,b,0,0), a, b > 0");
+  if (!(v.scale > 0.0f) || !std::isfinite(v.scale))
+    return Fail(SPH_ERR_INVALID, "scale must be positive and finite");
+  for (float x : v.view_proj)
+    if (!std::isfinite(x)) return Fail(SPH_ERR_INVALID, "view_proj must be finite");
+  if (pixels > render_pixels_) {
+    cudaFree(d_rkeys_);
+    cudaFree(d_rrgba_);
+    cudaFree(d_rdepth_);
+    d_rkeys_ = nullptr;
+    d_rrgba_ = nullptr;
+    d_rdepth_ = nullptr;
+    render_pixels_ = 0;
+    cudaError_t e = Alloc(&d_rkeys_, pixels);
+    if (e == cudaSuccess) e = Alloc(&d_rrgba_, pixels);
+    if (e == cudaSuccess) e = Alloc(&d_rdepth_, pixels);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return Fail(SPH_ERR_NOMEM, "render buffers do not fit the device");
+    }
+    render_pixels_ = pixels;
+  }
+  if (!d_rcolour_) SPH_CUDA(Alloc(&d_rcolour_, capacity_), "cudaMalloc");
+  RenderView rv{};
+  for (int k = 0; k < 16; ++k) rv.vp[k] = v.view_proj[k];
+  const float hs = 0.5f * v.scale;
+  rv.ox = P[0] * hs;
+  rv.oy = P[5] * hs;
+  rv.hw = 0.5f * static_cast<float>(v.width);
+  rv.hh = 0.5f * static_cast<float>(v.height);
+  rv.q = v.scale * 0.25f;
+  rv.width = v.width;
+  rv.height = v.height;
+  rv.clear = 0;
+  for (int k = 0; k < 4; ++k) {
+    const float c = std::fmin(std::fmax(v.clear[k], 0.0f), 1.0f) * 255.0f;
+    rv.clear |= static_cast<uint32_t>(std::lrint(c)) << (8 * k);
+  }
+  SPH_CUDA(launch_render(old_base_[id], scenes_[id].n, d_pos_[cur_], d_vel_[cur_], rv,
+                         d_rkeys_, d_rcolour_, d_rrgba_, d_rdepth_, st),
+           "render kernels");
+  if (rgba)
+    SPH_CUDA(cudaMemcpyAsync(rgba, d_rrgba_, 4 * pixels, cudaMemcpyDeviceToHost, st),
+             "download image");
+  if (depth)
+    SPH_CUDA(cudaMemcpyAsync(depth, d_rdepth_, 4 * pixels, cudaMemcpyDeviceToHost, st),
+             "download depth");
   SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   return SPH_OK;
 }

@@ -38,6 +38,9 @@ class Engine {
   int Download(uint32_t id, float* pos3, float* vel3, float* dens2,
                bool device_ptrs, cudaStream_t st);
   int OutPositions(uint32_t id, void** dev_float4);
+  // Headless render of scene `id`'s current state (sph_render); host outputs.
+  int Render(uint32_t id, const sph_view& view, uint8_t* rgba, float* depth,
+             cudaStream_t st);
   int DebugEnable(bool on);
   int DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
                   uint32_t* sorted_ids, uint32_t* start, float* dens2,
@@ -128,6 +131,14 @@ class Engine {
   uint32_t* d_dbg_tmp_ = nullptr;
   uint32_t* d_dbg_sorted_ = nullptr;
   void* d_dbg_scratch_ = nullptr;
+
+  // render buffers, grown on demand: (depth, index) keys, RGBA8 and depth per
+  // pixel, colour per particle
+  unsigned long long* d_rkeys_ = nullptr;
+  uint32_t* d_rrgba_ = nullptr;
+  float* d_rdepth_ = nullptr;
+  uint32_t* d_rcolour_ = nullptr;
+  uint64_t render_pixels_ = 0;
 
   // Neighbour-list capacity per particle (pairs with dist <= r); a particle
   // with more neighbours is handled by the bucket walk in the force passes.

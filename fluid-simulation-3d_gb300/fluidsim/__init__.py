@@ -2,12 +2,13 @@
 
 The compute path is libsph_gb300.so (hand-written sm_103a CUDA); this
 package only binds it (`_lib`), mirrors the reference's simulation class and
-plug-in (`simulation`) and builds the seeded benchmark scenes (`scenes`).
+plug-in (`simulation`), builds the seeded benchmark scenes (`scenes`) and
+the camera views of the headless render (`render`).
 """
-from . import scenes
+from . import render, scenes
 from ._lib import LIB_PATH, SphError, load
 from .simulation import (Batch, FluidSimCUDA, FluidSimulation, default_params,
                          grid_arrangement, to_params)
 
 __all__ = ["Batch", "FluidSimCUDA", "FluidSimulation", "SphError", "LIB_PATH",
-           "default_params", "grid_arrangement", "load", "scenes", "to_params"]
+           "default_params", "grid_arrangement", "load", "render", "scenes", "to_params"]

@@ -32,6 +32,7 @@ EXPORTS = (
     "sph_batch_profile_enable", "sph_batch_phase_times", "sph_set_tuning",
     "sph_get_tuning", "sph_autotune", "sph_spatial_lookup_static",
     "sph_static_error", "sph_bytes_per_particle", "sph_batch_sync",
+    "sph_render", "sph_batch_render",
 )
 STATIC_LOOKUP_MAX = 65536
 
@@ -60,6 +61,13 @@ class Tuning(ctypes.Structure):
                 ("force_block", ctypes.c_int32)]
 
 
+class View(ctypes.Structure):
+    """struct sph_view."""
+    _fields_ = [("view_proj", ctypes.c_float * 16), ("proj", ctypes.c_float * 16),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("scale", ctypes.c_float), ("clear", ctypes.c_float * 4)]
+
+
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
 _lib = None
@@ -81,6 +89,8 @@ def _sig(L):
         "sph_download": (i, [_P, _P, _P, _P, _P]),
         "sph_download_device": (i, [_P, _P, _P, _P, _P]),
         "sph_out_positions": (i, [_P, ctypes.POINTER(_P)]),
+        "sph_render": (i, [_P, ctypes.POINTER(View), _P, _P, _P]),
+        "sph_batch_render": (i, [_P, u32, ctypes.POINTER(View), _P, _P, _P]),
         "sph_debug_enable": (i, [_P, i]),
         "sph_debug_export": (i, [_P] + [_P] * 8 + [_P]),
         "sph_status": (i, [_P, ctypes.POINTER(u32), _P]),

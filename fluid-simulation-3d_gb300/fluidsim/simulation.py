@@ -163,6 +163,16 @@ class FluidSimulation:
         p = self._state()[0]
         return np.concatenate([p, np.full((self._n, 1), 0.34, np.float32)], axis=1)
 
+    def render(self, view):
+        """Headless render of the current state (sph_render): `view` is a
+        fluidsim.render.view(...). Returns (rgba uint8 [H, W, 4], depth
+        float32 [H, W]), rows bottom to top as glReadPixels gives them."""
+        rgba = np.empty((view.height, view.width, 4), np.uint8)
+        depth = np.empty((view.height, view.width), np.float32)
+        check(self._lib.sph_render(self._h, ctypes.byref(view), _ptr(rgba), _ptr(depth),
+                                   self._stream), self._h)
+        return rgba, depth
+
     def out_positions_device_ptr(self) -> int:
         """Device address of the headless float4 OutPositions buffer."""
         ptr = ctypes.c_void_p()
@@ -317,7 +327,9 @@ class FluidSimulation:
 
 class FluidSimCUDA:
     """FluidSimBase plug-in (fluidSimBase.h:5-14) driving FluidSimulation on
-    the GPU; render() hands back the headless OutPositions device buffer."""
+    the GPU. render() without a camera hands back the headless OutPositions
+    device buffer; with a camera view (fluidsim.render.view) it draws the
+    frame FluidSimCPU::render draws (fluidSimCPU.cc:53-93) headlessly."""
 
     def __init__(self, params=None, substeps: int = 1):
         self.sim = FluidSimulation(params)
@@ -337,8 +349,11 @@ class FluidSimCUDA:
     def cleanup(self):
         self.sim.close()
 
-    def render(self):
-        """Headless: (device pointer of float4[n] (pos, 0.34), n)."""
+    def render(self, view=None):
+        """Headless: (device pointer of float4[n] (pos, 0.34), n) without a
+        view; (rgba, depth) images of the frame with one."""
+        if view is not None:
+            return self.sim.render(view)
         return self.sim.out_positions_device_ptr(), self.nrParticles
 
 
@@ -406,6 +421,14 @@ class Batch:
         self._check(self._lib.sph_batch_download(self._h, int(sid), _ptr(pos), _ptr(vel),
                                                  _ptr(dens), self._stream))
         return pos, vel, dens
+
+    def render(self, sid: int, view):
+        """sph_batch_render of scene `sid`; see FluidSimulation.render."""
+        rgba = np.empty((view.height, view.width, 4), np.uint8)
+        depth = np.empty((view.height, view.width), np.float32)
+        self._check(self._lib.sph_batch_render(self._h, int(sid), ctypes.byref(view),
+                                               _ptr(rgba), _ptr(depth), self._stream))
+        return rgba, depth
 
     def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4,
                    force_block=0):

@@ -116,6 +116,29 @@ int sph_step(sph_sim *sim, float dt, int substeps, void *stream);
 int sph_download(sph_sim *sim, float *pos3, float *vel3, float *dens2,
                  void *stream);
 
+/* Headless render (replaces FluidSimCPU::render and updateColors,
+ * projects/Simulation/code/simulations/fluidSimCPU.cc:53-124, with the
+ * billboard shaders bin/shaders/particleRender.vs/.fs): every particle is a
+ * screen-aligned splat of size `scale` coloured by its speed, depth-tested
+ * with GL_LESS, into an RGBA8 image and its window depth. */
+typedef struct sph_view {
+  float view_proj[16]; /* cam.GetViewProjection() = P * V, column-major (glm) */
+  float proj[16];      /* cam.GetProjection(): columns 0 and 1 must be
+                          (a, 0, 0, 0) and (0, b, 0, 0) with a, b > 0, as
+                          glm::perspective / glm::ortho give              */
+  uint32_t width;      /* viewport in pixels, width * height <= 2^28      */
+  uint32_t height;
+  float scale;         /* billboard size: OutPositions.w = 0.34           */
+  float clear[4];      /* glClearColor, the app uses (0, 0, 0, 1)         */
+} sph_view;
+
+/* Render the current state. rgba: uint8[4 * width * height], depth:
+ * float[width * height] in [0, 1] (1 where no particle), rows bottom to
+ * top as glReadPixels returns them; host pointers, either may be NULL.
+ * Synchronises `stream`. */
+int sph_render(sph_sim *sim, const sph_view *view, uint8_t *rgba, float *depth,
+               void *stream);
+
 /* Device pointer to the headless OutPositions buffer (physicsWorld.h:80):
  * float4[n] = (position, 0.34) in the caller's order, refreshed by every
  * sph_step. Valid until sph_destroy. */
@@ -248,6 +271,10 @@ int sph_batch_step(sph_batch *b, int substeps, void *stream);
  * Synchronises `stream`. */
 int sph_batch_download(sph_batch *b, uint32_t scene_id, float *pos3,
                        float *vel3, float *dens2, void *stream);
+
+/* sph_render for one scene of the batch. */
+int sph_batch_render(sph_batch *b, uint32_t scene_id, const sph_view *view,
+                     uint8_t *rgba, float *depth, void *stream);
 
 /* Launch configuration of the batch's neighbour kernels and its autotuner
  * (see sph_tuning above). */

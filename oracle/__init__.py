@@ -5,7 +5,9 @@ may import this package. It wraps
 
   * oracle/_build/libsph_oracle.so -- the CPU restatement (sph_oracle.cc) of
     engine/physics/physicsWorld.cc:39-111,304-516 and kernels.h:25-82 of
-    Allkams/Fluid-Simulation-3D, built by `make -C oracle oracle`;
+    Allkams/Fluid-Simulation-3D, and of the frame its CPU plug-in draws
+    (sph_render_oracle.cc: fluidSimCPU.cc:53-124 with the particleRender
+    shaders), built by `make -C oracle oracle`;
   * oracle/_ref/ref_driver -- the reference's own physicsWorld.cc compiled
     unmodified with a stepwise driver (`make -C oracle ref`), present only
     where the reference sources exist (used to pin the restatement and to
@@ -83,6 +85,8 @@ def lib():
             ctypes.POINTER(OracleParams), ctypes.c_uint32, _P, ctypes.c_uint32,
             _P, ctypes.c_int, _P, _P, _P, _P, _P]
         L.sph_oracle_hw_threads.restype = ctypes.c_int
+        L.sph_oracle_render.argtypes = [_P, _P, ctypes.c_uint32, _P, _P, ctypes.c_uint32,
+                                        ctypes.c_uint32, ctypes.c_float, _P, _P, _P]
         _lib = L
     return _lib
 
@@ -247,3 +251,22 @@ def ref_update(params, pos, vel, dt, steps):
     ms = np.frombuffer(raw, np.float64, steps, o).copy(); o += 8 * steps
     phase = np.frombuffer(raw, np.float64, 6, o).copy()
     return posF, velF, dens, ms, phase
+
+
+def render(pos, vel, view):
+    """The frame sph_render draws, on the CPU: pos/vel (n, 3) in caller
+    order, `view` a fluidsim.render View. Returns (rgba [H, W, 4] uint8,
+    depth [H, W] float32)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    vel = np.ascontiguousarray(vel, dtype=np.float32)
+    vp = np.array(list(view.view_proj), np.float32)
+    pr = np.array(list(view.proj), np.float32)
+    clear = np.array(list(view.clear), np.float32)
+    rgba = np.empty((view.height, view.width, 4), np.uint8)
+    depth = np.empty((view.height, view.width), np.float32)
+    rc = lib().sph_oracle_render(_ptr(pos), _ptr(vel), pos.shape[0], _ptr(vp), _ptr(pr),
+                                 view.width, view.height, float(view.scale), _ptr(clear),
+                                 _ptr(rgba), _ptr(depth))
+    if rc != 0:
+        raise ValueError(f"oracle render failed: {rc}")
+    return rgba, depth

@@ -101,6 +101,15 @@ int sph_oracle_subset_f64(const oracle_params *p, uint32_t n, const float *pred,
                           double *out_dens, double *out_acc, double *out_abs,
                           double *out_sens, double *out_dsens);
 
+/* The headless render of sph_render (sph_render_oracle.cc): pos3/vel3 [3n]
+ * in caller order, vp = ViewProj and proj = Projection (column-major),
+ * rgba [4 * width * height] and depth [width * height] (either may be
+ * NULL), rows bottom to top. */
+int sph_oracle_render(const float *pos3, const float *vel3, uint32_t n,
+                      const float *vp, const float *proj, uint32_t width,
+                      uint32_t height, float scale, const float *clear,
+                      uint8_t *rgba, float *depth);
+
 /* Number of hardware threads the oracle would use for nthreads <= 0. */
 int sph_oracle_hw_threads(void);
 
