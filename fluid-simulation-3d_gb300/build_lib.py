@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libsph_gb300.so"
 SOURCES = ["sph_kernels.cu", "sph_engine.cu", "sph_capi.cu", "sph_static.cu",
-           "sph_render.cu"]
+           "sph_render.cu", "sph_snapshot.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -131,6 +131,20 @@ int sph_download_device(sph_sim* sim, float* dpos3, float* dvel3, float* ddens2,
   return sim->eng.Download(sim->scene, dpos3, dvel3, ddens2, true, S(stream));
 }
 
+int sph_save(sph_sim* sim, const char* path, void* stream) {
+  if (!sim || !path) return SPH_ERR_INVALID;
+  return sim->eng.SaveSnapshot(sim->scene, path, S(stream));
+}
+
+int sph_load(sph_sim* sim, const char* path, void* stream) {
+  if (!sim || !path) return SPH_ERR_INVALID;
+  sph::SceneSnapshot snap;
+  int rc = sim->eng.ReadSnapshot(path, &snap);
+  if (rc == SPH_OK) rc = sim->eng.RestoreSnapshot(sim->scene, snap, S(stream));
+  if (rc == SPH_OK) sim->prm = snap.prm;
+  return rc;
+}
+
 int sph_render(sph_sim* sim, const sph_view* view, uint8_t* rgba, float* depth,
                void* stream) {
   if (!sim || !view) return SPH_ERR_INVALID;
@@ -245,6 +259,19 @@ int sph_batch_download(sph_batch* b, uint32_t scene_id, float* pos3,
                        float* vel3, float* dens2, void* stream) {
   if (!b) return SPH_ERR_INVALID;
   return b->eng.Download(scene_id, pos3, vel3, dens2, false, S(stream));
+}
+
+int sph_batch_save(sph_batch* b, uint32_t scene_id, const char* path, void* stream) {
+  if (!b || !path) return SPH_ERR_INVALID;
+  return b->eng.SaveSnapshot(scene_id, path, S(stream));
+}
+
+int sph_batch_add_snapshot(sph_batch* b, const char* path, uint32_t* scene_id,
+                           void* stream) {
+  if (!b || !path) return SPH_ERR_INVALID;
+  sph::SceneSnapshot snap;
+  const int rc = b->eng.ReadSnapshot(path, &snap);
+  return rc == SPH_OK ? b->eng.AddSnapshot(snap, scene_id, S(stream)) : rc;
 }
 
 int sph_batch_render(sph_batch* b, uint32_t scene_id, const sph_view* view,

@@ -16,6 +16,13 @@
 
 namespace sph {
 
+// A scene's state and settings as a snapshot file holds them (caller order).
+struct SceneSnapshot {
+  sph_params prm{};
+  float dt = 0.0f;
+  std::vector<float> pos, vel, dens;  // [3n], [3n], [2n]
+};
+
 class Engine {
  public:
   Engine(uint64_t capacity, uint32_t max_scenes);
@@ -38,6 +45,13 @@ class Engine {
   int Download(uint32_t id, float* pos3, float* vel3, float* dens2,
                bool device_ptrs, cudaStream_t st);
   int OutPositions(uint32_t id, void** dev_float4);
+  // Snapshots (sph_snapshot.cu): write scene `id` to a file, read a file,
+  // put a snapshot into an existing scene of the same size, or add it as a
+  // new scene.
+  int SaveSnapshot(uint32_t id, const char* path, cudaStream_t st);
+  int ReadSnapshot(const char* path, SceneSnapshot* s);
+  int RestoreSnapshot(uint32_t id, const SceneSnapshot& s, cudaStream_t st);
+  int AddSnapshot(const SceneSnapshot& s, uint32_t* id, cudaStream_t st);
   // Headless render of scene `id`'s current state (sph_render); host outputs.
   int Render(uint32_t id, const sph_view& view, uint8_t* rgba, float* depth,
              cudaStream_t st);

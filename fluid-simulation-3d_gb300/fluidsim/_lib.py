@@ -32,7 +32,8 @@ EXPORTS = (
     "sph_batch_profile_enable", "sph_batch_phase_times", "sph_set_tuning",
     "sph_get_tuning", "sph_autotune", "sph_spatial_lookup_static",
     "sph_static_error", "sph_bytes_per_particle", "sph_batch_sync",
-    "sph_render", "sph_batch_render",
+    "sph_render", "sph_batch_render", "sph_save", "sph_load", "sph_batch_save",
+    "sph_batch_add_snapshot",
 )
 STATIC_LOOKUP_MAX = 65536
 
@@ -91,6 +92,10 @@ def _sig(L):
         "sph_out_positions": (i, [_P, ctypes.POINTER(_P)]),
         "sph_render": (i, [_P, ctypes.POINTER(View), _P, _P, _P]),
         "sph_batch_render": (i, [_P, u32, ctypes.POINTER(View), _P, _P, _P]),
+        "sph_save": (i, [_P, ctypes.c_char_p, _P]),
+        "sph_load": (i, [_P, ctypes.c_char_p, _P]),
+        "sph_batch_save": (i, [_P, u32, ctypes.c_char_p, _P]),
+        "sph_batch_add_snapshot": (i, [_P, ctypes.c_char_p, ctypes.POINTER(u32), _P]),
         "sph_debug_enable": (i, [_P, i]),
         "sph_debug_export": (i, [_P] + [_P] * 8 + [_P]),
         "sph_status": (i, [_P, ctypes.POINTER(u32), _P]),

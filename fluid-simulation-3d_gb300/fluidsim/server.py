@@ -10,9 +10,11 @@ run share the device with them. A request leaves, with its final state read
 back, after its K-th step. A request can be withdrawn with cancel() (for
 instance from the per-step callback): it is dropped if it has not been
 admitted, and a resident one leaves the batch at the next step boundary,
-freeing its capacity for the requests still waiting. The loop records each
-request's per-step latency: the wall time of the batched step it took part
-in, measured with a stream sync around the step.
+freeing its capacity for the requests still waiting. checkpoint() persists
+the loop between steps (scene snapshots of the resident requests, the queue,
+the finished results); resume() turns that into requests for a new loop.
+The loop records each request's per-step latency: the wall time of the
+batched step it took part in, measured with a stream sync around the step.
 
 The batched step runs the same per-particle arithmetic in the same order as a
 scene stepped alone, so every result is the same alone and in the mix (the
@@ -21,12 +23,14 @@ GPU tests check it bit for bit).
 from __future__ import annotations
 
 import dataclasses
+import json
+import os
 import time
 
 import numpy as np
 
-from . import _lib
-from .simulation import Batch, FluidSimulation
+from . import _lib, snapshot
+from .simulation import Batch, FluidSimulation, to_params
 
 
 @dataclasses.dataclass
@@ -39,6 +43,7 @@ class Request:
     substeps: int
     steps: int
     arrival: float = 0.0  # seconds after the loop starts
+    snapshot: str | None = None  # resumed: admitted from this scene snapshot
 
     @property
     def n(self) -> int:
@@ -93,10 +98,20 @@ class Server:
             cancelled.append(req.rid)
         self._cancel.clear()
 
+    def _try_add(self, req):
+        if req.snapshot is None:
+            return self.batch.try_add(req.params, req.pos, req.vel, req.dt)
+        try:
+            return self.batch.add_snapshot(req.snapshot)
+        except _lib.SphError as e:
+            if e.code == -3:
+                return None
+            raise
+
     def _admit(self, waiting, now):
         admitted = []
         for req in list(waiting):
-            sid = self.batch.try_add(req.params, req.pos, req.vel, req.dt)
+            sid = self._try_add(req)
             if sid is None:
                 continue  # does not fit now; a smaller later one may
             self.resident[sid] = [req, req.steps, now, []]
@@ -114,6 +129,8 @@ class Server:
             raise ValueError("one substep count per server")
         substeps = substeps.pop() if substeps else 1
         waiting, done, cancelled = [], {}, []
+        self._run_state = dict(pending=pending, waiting=waiting, done=done,
+                               substeps=substeps, t0=time.perf_counter(), offset=0.0)
         t0 = time.perf_counter()
         offset = 0.0  # time skipped while idle (realtime=False)
         lat, steps, pstep = [], 0, 0
@@ -131,6 +148,7 @@ class Server:
                         time.sleep(max(0.0, gap))
                     else:
                         offset += max(0.0, gap)
+                        self._run_state["offset"] = offset
                     continue
                 if waiting:
                     raise RuntimeError(f"request {waiting[0].rid} ({waiting[0].n} particles) "
@@ -170,6 +188,72 @@ class Server:
             capacity_particles=int(self.capacity),
         )
         return done, stats
+
+
+    def checkpoint(self, directory) -> None:
+        """Persist the loop between two steps (call it from run()'s on_step):
+        every resident request's scene as a snapshot file with its steps left,
+        the requests not admitted yet (initial state and settings), and the
+        finished results, under `directory` with a manifest.json. resume()
+        turns it back into requests and results; a new Server run on them
+        finishes every request exactly as the uninterrupted loop would."""
+        st = getattr(self, "_run_state", None)
+        if st is None:
+            raise RuntimeError("checkpoint() is called from inside run()")
+        os.makedirs(directory, exist_ok=True)
+        now = time.perf_counter() - st["t0"] + st["offset"]
+        man = dict(version=1, substeps=st["substeps"], time=now, resident=[], queued=[],
+                   done=[])
+        for sid, (req, left, adm, sm) in self.resident.items():
+            name = f"r{req.rid}.sph"
+            self.batch.save(sid, os.path.join(directory, name))
+            man["resident"].append(dict(rid=req.rid, steps=left, file=name, step_ms=sm))
+        for req in list(st["waiting"]) + list(st["pending"]):
+            name = f"q{req.rid}.npz"
+            p = to_params(req.params)
+            np.savez(os.path.join(directory, name), pos=req.pos, vel=req.vel)
+            man["queued"].append(dict(
+                rid=req.rid, steps=req.steps, file=name, dt=req.dt, arrival=req.arrival,
+                params={k: (list(getattr(p, k)) if k == "bound" else getattr(p, k))
+                        for k, _ in p._fields_}))
+        for rid, d in st["done"].items():
+            name = f"d{rid}.npz"
+            np.savez(os.path.join(directory, name), pos=d.pos, vel=d.vel, dens=d.dens)
+            man["done"].append(dict(rid=rid, file=name, admitted=d.admitted,
+                                    finished=d.finished, step_ms=d.step_ms))
+        with open(os.path.join(directory, "manifest.json"), "w") as f:
+            json.dump(man, f)
+
+
+def resume(directory):
+    """The requests and results of a Server.checkpoint(): (requests, done)
+    -- resident requests resume from their scene snapshots with their steps
+    left, queued ones keep their arrival offset relative to the checkpoint."""
+    with open(os.path.join(directory, "manifest.json")) as f:
+        man = json.load(f)
+    S = man["substeps"]
+    reqs, done = [], {}
+    for r in man["resident"]:
+        path = os.path.join(directory, r["file"])
+        snap = snapshot.read(path)
+        reqs.append(Request(r["rid"], snap["params"], snap["pos"], snap["vel"], snap["dt"],
+                            S, r["steps"], arrival=0.0, snapshot=path))
+    for q in man["queued"]:
+        a = np.load(os.path.join(directory, q["file"]))
+        p = _lib.Params()
+        for k, v in q["params"].items():
+            if k == "bound":
+                for i in range(3):
+                    p.bound[i] = v[i]
+            else:
+                setattr(p, k, v)
+        reqs.append(Request(q["rid"], p, a["pos"], a["vel"], q["dt"], S, q["steps"],
+                            arrival=max(0.0, q["arrival"] - man["time"])))
+    for d in man["done"]:
+        a = np.load(os.path.join(directory, d["file"]))
+        done[d["rid"]] = Done(d["rid"], a["pos"], a["vel"], a["dens"], d["admitted"],
+                              d["finished"], d["step_ms"])
+    return reqs, done
 
 
 def run_alone(req: Request, stream=None, tuning=None):

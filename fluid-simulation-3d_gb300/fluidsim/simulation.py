@@ -163,6 +163,17 @@ class FluidSimulation:
         p = self._state()[0]
         return np.concatenate([p, np.full((self._n, 1), 0.34, np.float32)], axis=1)
 
+    def save(self, path):
+        """Snapshot the state and settings to `path` (sph_save)."""
+        check(self._lib.sph_save(self._h, str(path).encode(), self._stream), self._h)
+
+    def load(self, path):
+        """Replace the state and settings with a snapshot of the same
+        particle count (sph_load)."""
+        check(self._lib.sph_load(self._h, str(path).encode(), self._stream), self._h)
+        check(self._lib.sph_get_params(self._h, ctypes.byref(self._params)), self._h)
+        self._cache = None
+
     def render(self, view):
         """Headless render of the current state (sph_render): `view` is a
         fluidsim.render.view(...). Returns (rgba uint8 [H, W, 4], depth
@@ -406,6 +417,22 @@ class Batch:
     def remove(self, sid: int):
         self._check(self._lib.sph_batch_remove(self._h, int(sid)))
         self.sizes.pop(int(sid), None)
+
+    def save(self, sid: int, path):
+        """Snapshot scene `sid` to `path` (sph_batch_save)."""
+        self._check(self._lib.sph_batch_save(self._h, int(sid), str(path).encode(),
+                                             self._stream))
+
+    def add_snapshot(self, path) -> int:
+        """Add a saved scene (sph_batch_add_snapshot); returns its id."""
+        with open(path, "rb") as f:
+            head = f.read(16)
+        n = int(np.frombuffer(head[12:16], np.uint32)[0]) if len(head) == 16 else 0
+        sid = ctypes.c_uint32()
+        self._check(self._lib.sph_batch_add_snapshot(self._h, str(path).encode(),
+                                                     ctypes.byref(sid), self._stream))
+        self.sizes[int(sid.value)] = n
+        return int(sid.value)
 
     def step(self, substeps: int):
         self._check(self._lib.sph_batch_step(self._h, int(substeps), self._stream))

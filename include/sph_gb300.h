@@ -116,6 +116,16 @@ int sph_step(sph_sim *sim, float dt, int substeps, void *stream);
 int sph_download(sph_sim *sim, float *pos3, float *vel3, float *dens2,
                  void *stream);
 
+/* Snapshots: the state (positions, velocities, densities, in the caller's
+ * order) and settings (sph_params and the step dt) of a scene in a binary
+ * file, for checkpoint / resume (the reference has no state I/O). The file
+ * is little-endian, 80 header bytes + 32 bytes per particle, with a
+ * checksum; a loaded scene continues bit for bit as if it had never been
+ * saved. sph_load needs a file of the handle's particle count and replaces
+ * its settings and state. Both synchronise `stream`. */
+int sph_save(sph_sim *sim, const char *path, void *stream);
+int sph_load(sph_sim *sim, const char *path, void *stream);
+
 /* Headless render (replaces FluidSimCPU::render and updateColors,
  * projects/Simulation/code/simulations/fluidSimCPU.cc:53-124, with the
  * billboard shaders bin/shaders/particleRender.vs/.fs): every particle is a
@@ -271,6 +281,12 @@ int sph_batch_step(sph_batch *b, int substeps, void *stream);
  * Synchronises `stream`. */
 int sph_batch_download(sph_batch *b, uint32_t scene_id, float *pos3,
                        float *vel3, float *dens2, void *stream);
+
+/* Snapshot one scene of the batch to a file, or add a saved scene to the
+ * batch (SPH_ERR_NOMEM when it does not fit). */
+int sph_batch_save(sph_batch *b, uint32_t scene_id, const char *path, void *stream);
+int sph_batch_add_snapshot(sph_batch *b, const char *path, uint32_t *scene_id,
+                           void *stream);
 
 /* sph_render for one scene of the batch. */
 int sph_batch_render(sph_batch *b, uint32_t scene_id, const sph_view *view,
