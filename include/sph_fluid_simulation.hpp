@@ -131,6 +131,29 @@ class FluidSimulation {
   void setCollisionDamping(float v) { prm_.damping = v; Push(); }
   void setPredictionDt(float v) { prm_.predict_dt = v; Push(); }
 
+  // Snapshot of the state and settings (sph_save / sph_load); Load needs a
+  // file of this simulation's particle count and refreshes the host mirrors.
+  void Save(const std::string& path) {
+    Require();
+    Check(sph_save(h_, path.c_str(), stream_), h_);
+  }
+  void Load(const std::string& path) {
+    Require();
+    Check(sph_load(h_, path.c_str(), stream_), h_);
+    Check(sph_get_params(h_, &prm_), h_);
+    Download();
+  }
+
+  // Headless frame (sph_render): rgba gets 4 * width * height bytes, depth
+  // (optional) width * height floats, rows bottom to top.
+  void Render(const sph_view& view, std::vector<uint8_t>& rgba,
+              std::vector<float>* depth = nullptr) {
+    Require();
+    rgba.resize(4ull * view.width * view.height);
+    if (depth) depth->resize(static_cast<size_t>(view.width) * view.height);
+    Check(sph_render(h_, &view, rgba.data(), depth ? depth->data() : nullptr, stream_), h_);
+  }
+
   uint32_t numParticles() const { return n_; }
   sph_sim* handle() const { return h_; }
   void setStream(void* s) { stream_ = s; }
@@ -213,6 +236,22 @@ class FluidSimCUDA {
     void* p = nullptr;
     if (sph_out_positions(sim_.handle(), &p) != SPH_OK) return nullptr;
     return p;
+  }
+  // The frame FluidSimCPU::render draws (fluidSimCPU.cc:53-93) for a camera:
+  // view_proj = cam.GetViewProjection(), proj = cam.GetProjection()
+  // (column-major, glm::value_ptr), cleared to black as the app does.
+  void render(const float* view_proj, const float* proj, uint32_t width, uint32_t height,
+              std::vector<uint8_t>& rgba, std::vector<float>* depth = nullptr) {
+    sph_view v{};
+    for (int k = 0; k < 16; ++k) {
+      v.view_proj[k] = view_proj[k];
+      v.proj[k] = proj[k];
+    }
+    v.width = width;
+    v.height = height;
+    v.scale = 0.34f;
+    v.clear[3] = 1.0f;
+    sim_.Render(v, rgba, depth);
   }
 
  private:

@@ -30,8 +30,8 @@ def test_cpp_mirror_compiles_and_links(built_lib, tmp_path):
 @pytest.mark.gpu
 def test_cpp_mirror_runs(gpu_lib, built_lib, tmp_path):
     exe = build_host_program(built_lib, tmp_path)
-    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120,
-                       env=dict(os.environ))
+    env = dict(os.environ, SPH_SNAPSHOT_PATH=str(tmp_path / "host.sph"))
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120, env=env)
     print(r.stdout, r.stderr)
     assert r.returncode == 0
     assert r.stdout.startswith("ok")
