@@ -82,55 +82,98 @@ __device__ __forceinline__ float row_dot(const float* m, int r, float x, float y
   return fa(fa(fm(m[r], x), fm(m[4 + r], y)), fa(fm(m[8 + r], z), m[12 + r]));
 }
 
-// Thread per particle of the scene's slots [first, first + n): its colour
-// (by caller index) and its splat into the (depth, index) buffer.
+// Pixels of one splat from row ya, column xa, in a (xb - xa + 1)-wide box,
+// visited from index `start` with stride `step`: the discard test and the
+// depth test of particleRender.fs for each pixel centre.
+__device__ __forceinline__ void splat_pixels(const RenderView& v, int xa, int xb, int ya, int yb,
+                                             float x0, float x1, float y0, float y1,
+                                             unsigned long long key, int start, int step,
+                                             unsigned long long* __restrict__ keys) {
+  const float dx = fs(x1, x0), dy = fs(y1, y0);
+  const float two_ox = fa(v.ox, v.ox), two_oy = fa(v.oy, v.oy);
+  const int w = xb - xa + 1, area = w * (yb - ya + 1);
+  for (int t = start; t < area; t += step) {
+    const int py = ya + t / w, px = xa + t % w;
+    const float fy = fd(fs(fa(static_cast<float>(py), 0.5f), y0), dy);
+    const float vy = fs(fm(fy, two_oy), v.oy);
+    const float fx = fd(fs(fa(static_cast<float>(px), 0.5f), x0), dx);
+    const float vx = fs(fm(fx, two_ox), v.ox);
+    if (__fsqrt_rn(fa(fm(vx, vx), fm(vy, vy))) > v.q) continue;  // discard
+    atomicMin(keys + static_cast<uint64_t>(py) * v.width + px, key);
+  }
+}
+
+// Particles of the scene's slots [first, first + n), one per thread: its
+// colour (by caller index) and its splat into the (depth, index) buffer.
+// A splat of more than kWarpSplat pixels (a particle close to the camera)
+// is drawn by the whole warp, the lanes taking its pixels in turn.
+constexpr int kWarpSplat = 64;
+
 __global__ void k_splat(uint32_t first, uint32_t n, const float4* __restrict__ pos,
                         const float4* __restrict__ vel, RenderView v,
                         unsigned long long* __restrict__ keys,
                         uint32_t* __restrict__ colours) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  const float4 p = pos[first + k];
-  const uint32_t id = __float_as_uint(p.w);
-  if (id >= n) return;
-  const float4 vv = vel[first + k];
-  colours[id] = speed_colour(vv.x, vv.y, vv.z);
-  const float cx = row_dot(v.vp, 0, p.x, p.y, p.z);
-  const float cy = row_dot(v.vp, 1, p.x, p.y, p.z);
-  const float cz = row_dot(v.vp, 2, p.x, p.y, p.z);
-  const float cw = row_dot(v.vp, 3, p.x, p.y, p.z);
-  if (!(cw > 0.0f) || !(cz >= -cw && cz <= cw)) return;  // behind / outside near-far
-  const float x0 = fa(fm(fd(fs(cx, v.ox), cw), v.hw), v.hw);
-  const float x1 = fa(fm(fd(fa(cx, v.ox), cw), v.hw), v.hw);
-  const float y0 = fa(fm(fd(fs(cy, v.oy), cw), v.hh), v.hh);
-  const float y1 = fa(fm(fd(fa(cy, v.oy), cw), v.hh), v.hh);
-  if (!(x1 > x0) || !(y1 > y0)) return;  // degenerate (also NaN)
-  const float depth = fa(fm(fd(cz, cw), 0.5f), 0.5f);
-  // covered centres: x0 <= px + 1/2 < x1, y0 < py + 1/2 <= y1; clamped to
-  // the image in float before the integer conversion
-  const float fw = static_cast<float>(v.width), fh = static_cast<float>(v.height);
-  const int px0 = static_cast<int>(ceilf(fminf(fmaxf(fs(x0, 0.5f), -1.0f), fw)));
-  const int px1 = static_cast<int>(ceilf(fminf(fmaxf(fs(x1, 0.5f), -1.0f), fw))) - 1;
-  const int py0 = static_cast<int>(floorf(fminf(fmaxf(fs(y0, 0.5f), -1.0f), fh))) + 1;
-  const int py1 = static_cast<int>(floorf(fminf(fmaxf(fs(y1, 0.5f), -1.0f), fh)));
-  const int xa = max(px0, 0), xb = min(px1, static_cast<int>(v.width) - 1);
-  const int ya = max(py0, 0), yb = min(py1, static_cast<int>(v.height) - 1);
-  if (xa > xb || ya > yb) return;
-  const float dx = fs(x1, x0), dy = fs(y1, y0);
-  const float two_ox = fa(v.ox, v.ox), two_oy = fa(v.oy, v.oy);
+  const uint32_t lane = threadIdx.x & 31u;
+  bool live = k < n;
+  uint32_t id = 0;
+  float4 p = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (live) {
+    p = pos[first + k];
+    id = __float_as_uint(p.w);
+    live = id < n;
+  }
+  if (live) {
+    const float4 vv = vel[first + k];
+    colours[id] = speed_colour(vv.x, vv.y, vv.z);
+  }
+  float x0 = 0.0f, x1 = 0.0f, y0 = 0.0f, y1 = 0.0f, depth = 0.0f;
+  if (live) {
+    const float cx = row_dot(v.vp, 0, p.x, p.y, p.z);
+    const float cy = row_dot(v.vp, 1, p.x, p.y, p.z);
+    const float cz = row_dot(v.vp, 2, p.x, p.y, p.z);
+    const float cw = row_dot(v.vp, 3, p.x, p.y, p.z);
+    live = cw > 0.0f && cz >= -cw && cz <= cw;  // else behind / outside near-far
+    if (live) {
+      x0 = fa(fm(fd(fs(cx, v.ox), cw), v.hw), v.hw);
+      x1 = fa(fm(fd(fa(cx, v.ox), cw), v.hw), v.hw);
+      y0 = fa(fm(fd(fs(cy, v.oy), cw), v.hh), v.hh);
+      y1 = fa(fm(fd(fa(cy, v.oy), cw), v.hh), v.hh);
+      depth = fa(fm(fd(cz, cw), 0.5f), 0.5f);
+      live = x1 > x0 && y1 > y0;  // degenerate (also NaN)
+    }
+  }
+  // covered centres: x0 <= px + 1/2 < x1, y0 < py + 1/2 <= y1; clamped to the
+  // image in float before the integer conversion
+  int xa = 0, xb = -1, ya = 0, yb = -1;
+  if (live) {
+    const float fw = static_cast<float>(v.width), fh = static_cast<float>(v.height);
+    const int px0 = static_cast<int>(ceilf(fminf(fmaxf(fs(x0, 0.5f), -1.0f), fw)));
+    const int px1 = static_cast<int>(ceilf(fminf(fmaxf(fs(x1, 0.5f), -1.0f), fw))) - 1;
+    const int py0 = static_cast<int>(floorf(fminf(fmaxf(fs(y0, 0.5f), -1.0f), fh))) + 1;
+    const int py1 = static_cast<int>(floorf(fminf(fmaxf(fs(y1, 0.5f), -1.0f), fh)));
+    xa = max(px0, 0);
+    xb = min(px1, static_cast<int>(v.width) - 1);
+    ya = max(py0, 0);
+    yb = min(py1, static_cast<int>(v.height) - 1);
+    live = xa <= xb && ya <= yb;
+  }
   const unsigned long long key =
       (static_cast<unsigned long long>(__float_as_uint(depth)) << 32) | id;
-  for (int py = ya; py <= yb; ++py) {
-    const float fy = fd(fs(fa(static_cast<float>(py), 0.5f), y0), dy);
-    const float vy = fs(fm(fy, two_oy), v.oy);
-    const float vy2 = fm(vy, vy);
-    unsigned long long* row = keys + static_cast<uint64_t>(py) * v.width;
-    for (int px = xa; px <= xb; ++px) {
-      const float fx = fd(fs(fa(static_cast<float>(px), 0.5f), x0), dx);
-      const float vx = fs(fm(fx, two_ox), v.ox);
-      if (__fsqrt_rn(fa(fm(vx, vx), vy2)) > v.q) continue;  // discard
-      atomicMin(row + px, key);
-    }
+  const bool big = live && (xb - xa + 1) * (yb - ya + 1) > kWarpSplat;
+  if (live && !big) splat_pixels(v, xa, xb, ya, yb, x0, x1, y0, y1, key, 0, 1, keys);
+  // large splats, one at a time across the warp (every lane arrives here)
+  for (uint32_t m = __ballot_sync(0xffffffffu, big); m; m &= m - 1u) {
+    const int src = __ffs(m) - 1;
+    const int bxa = __shfl_sync(0xffffffffu, xa, src), bxb = __shfl_sync(0xffffffffu, xb, src);
+    const int bya = __shfl_sync(0xffffffffu, ya, src), byb = __shfl_sync(0xffffffffu, yb, src);
+    const float bx0 = __shfl_sync(0xffffffffu, x0, src), bx1 = __shfl_sync(0xffffffffu, x1, src);
+    const float by0 = __shfl_sync(0xffffffffu, y0, src), by1 = __shfl_sync(0xffffffffu, y1, src);
+    const uint32_t klo = __shfl_sync(0xffffffffu, static_cast<uint32_t>(key), src);
+    const uint32_t khi = __shfl_sync(0xffffffffu, static_cast<uint32_t>(key >> 32), src);
+    const unsigned long long bkey = (static_cast<unsigned long long>(khi) << 32) | klo;
+    splat_pixels(v, bxa, bxb, bya, byb, bx0, bx1, by0, by1, bkey, static_cast<int>(lane), 32,
+                 keys);
   }
 }
 
