@@ -627,7 +627,8 @@ def run_served(args):
         sc = scenes.request_scene(rng)
         reqs.append(server.Request(len(reqs), sc["params"], sc["pos"], sc["vel"],
                                    sc["dt"], sc["substeps"], sc["steps"], arrival=t))
-    srv = server.Server(64 << 30, max_scenes=8192)
+    # the library's own serving loop (sph_server_*, a C++ worker thread)
+    srv = server.NativeServer(64 << 30, max_scenes=8192, substeps=reqs[0].substeps)
     done, stats = srv.run(reqs, realtime=True)
     srv.close()
     # serial plain launches on a sample of the same stream
@@ -643,7 +644,8 @@ def run_served(args):
         "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded request stream)",
         "config": {"workload": "served", "rate_per_s": 200, "seconds": args.serve_seconds,
-                   "requests": len(reqs), "budget_bytes": 64 << 30},
+                   "requests": len(reqs), "budget_bytes": 64 << 30,
+                   "server": "sph_server (native loop on a worker thread)"},
         "p50_step_ms": stats["p50_step_ms"], "p99_step_ms": stats["p99_step_ms"],
         "served": stats,
         "serial_plain": {"value": serial, "sample_requests": len(sample)},

@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libsph_gb300.so"
 SOURCES = ["sph_kernels.cu", "sph_engine.cu", "sph_capi.cu", "sph_static.cu",
-           "sph_render.cu", "sph_snapshot.cu"]
+           "sph_render.cu", "sph_snapshot.cu", "sph_server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -52,7 +52,7 @@ def build(extra=(), force: bool = False) -> pathlib.Path:
     with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, list(extra)), SOURCES))
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs),
-           "-lcudart"]
+           "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}{r.stderr}")

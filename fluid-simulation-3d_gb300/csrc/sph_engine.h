@@ -77,6 +77,7 @@ class Engine {
   void UseGraphs(bool on) { use_graphs_ = on; }
   uint32_t NumScenes() const;
   uint64_t NumParticles() const;
+  uint64_t Capacity() const { return capacity_; }
   uint32_t SceneSize(uint32_t id) const;
   const char* LastError() const { return err_.c_str(); }
   int Fail(int code, const std::string& msg);

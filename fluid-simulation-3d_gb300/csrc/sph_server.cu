@@ -1,0 +1,329 @@
+// Native serving loop (sph_server_*): continuous batching of scene jobs over
+// one batch engine, on a worker thread. Any thread submits a job (a scene of
+// n particles to advance K steps), cancels it or waits for its result; the
+// worker admits waiting jobs in submission order while the HBM budget has
+// room (later, smaller jobs may backfill), advances every resident scene one
+// step per batched launch, and retires a job after its K-th step with its
+// state read back. The engine is only touched by the worker, and the job
+// queue only under the server's mutex. Results equal the job run alone, bit
+// for bit: a batched step runs every particle's arithmetic in the same order
+// as a single-scene step.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/sph_gb300.h"
+#include "sph_engine.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Job {
+  uint64_t id = 0;
+  sph_params prm{};
+  uint32_t n = 0;
+  float dt = 0.0f;
+  uint32_t steps_left = 0;
+  std::vector<float> pos, vel, dens;  // inputs, then the results
+  uint32_t scene = 0;
+  bool resident = false, done = false, cancel = false;
+  int status = SPH_OK;  // SPH_OK, or why the job ended without a result
+  std::string why;
+};
+
+double Seconds(Clock::time_point a, Clock::time_point b) {
+  return std::chrono::duration<double>(b - a).count();
+}
+
+}  // namespace
+
+struct sph_server {
+  sph::Engine eng;
+  int substeps;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::condition_variable work_cv, done_cv;
+  std::deque<std::shared_ptr<Job>> waiting;
+  std::map<uint32_t, std::shared_ptr<Job>> resident;  // scene id -> job
+  std::map<uint64_t, std::shared_ptr<Job>> jobs;      // not yet collected
+  uint64_t next_id = 1;
+  bool stop = false;
+  std::thread worker;
+  // statistics (under mu)
+  uint64_t submitted = 0, completed = 0, cancelled = 0, failed = 0;
+  uint64_t steps = 0, particle_steps = 0;
+  std::vector<std::pair<float, uint32_t>> step_ms;  // (ms, jobs it advanced)
+  bool started = false;
+  Clock::time_point t_first{}, t_last{};
+  std::string err;
+
+  sph_server(uint64_t capacity, uint32_t max_scenes, int ss)
+      : eng(capacity, max_scenes), substeps(ss) {}
+
+  void Finish(const std::shared_ptr<Job>& j, int status, const std::string& why) {
+    j->done = true;
+    j->status = status;
+    j->why = why;
+    if (status == SPH_OK) {
+      ++completed;
+    } else {
+      if (j->cancel) ++cancelled;
+      else ++failed;
+      std::vector<float>().swap(j->pos);
+      std::vector<float>().swap(j->vel);
+    }
+    done_cv.notify_all();
+  }
+
+  // Admission and cancellation of resident jobs; called by the worker with
+  // mu held.
+  void Admit() {
+    for (auto it = resident.begin(); it != resident.end();) {
+      if (it->second->cancel) {
+        eng.RemoveScene(it->first);
+        Finish(it->second, SPH_ERR_STATE, "cancelled");
+        it = resident.erase(it);
+      } else {
+        ++it;
+      }
+    }
+    for (auto it = waiting.begin(); it != waiting.end();) {
+      const std::shared_ptr<Job>& j = *it;
+      uint32_t sid = 0;
+      const int rc = eng.AddScene(j->prm, j->n, j->pos.data(),
+                                  j->vel.empty() ? nullptr : j->vel.data(), false, j->dt,
+                                  &sid, stream);
+      if (rc == SPH_ERR_NOMEM) {  // no room now; a smaller later job may fit
+        ++it;
+        continue;
+      }
+      if (rc != SPH_OK) {
+        Finish(j, rc, eng.LastError());
+      } else {
+        j->scene = sid;
+        j->resident = true;
+        std::vector<float>().swap(j->vel);
+        resident[sid] = j;
+        if (!started) {
+          started = true;
+          t_first = Clock::now();
+        }
+      }
+      it = waiting.erase(it);
+    }
+    if (resident.empty() && !waiting.empty()) {
+      // nothing runs and nothing fits: these jobs can never be admitted
+      for (auto& j : waiting) Finish(j, SPH_ERR_NOMEM, "job does not fit the server's budget");
+      waiting.clear();
+    }
+  }
+
+  void Run() {
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    while (true) {
+      work_cv.wait(lk, [&] { return stop || !waiting.empty() || !resident.empty(); });
+      if (stop) {
+        for (auto& j : waiting) Finish(j, SPH_ERR_STATE, "server stopped");
+        for (auto& kv : resident) Finish(kv.second, SPH_ERR_STATE, "server stopped");
+        waiting.clear();
+        resident.clear();
+        break;
+      }
+      Admit();
+      if (resident.empty()) continue;
+      uint64_t live = 0;
+      for (auto& kv : resident) live += kv.second->n;
+      const uint32_t nres = static_cast<uint32_t>(resident.size());
+      lk.unlock();  // submitters and waiters run while the step does
+      const Clock::time_point t0 = Clock::now();
+      int rc = eng.Step(substeps, stream);
+      if (rc == SPH_OK && cudaStreamSynchronize(stream) != cudaSuccess) rc = SPH_ERR_CUDA;
+      const Clock::time_point t1 = Clock::now();
+      lk.lock();
+      if (rc != SPH_OK) {
+        err = eng.LastError();
+        for (auto& kv : resident) {
+          eng.RemoveScene(kv.first);
+          Finish(kv.second, rc, err);
+        }
+        resident.clear();
+        continue;
+      }
+      ++steps;
+      particle_steps += live;
+      step_ms.emplace_back(static_cast<float>(1000.0 * Seconds(t0, t1)), nres);
+      t_last = t1;
+      for (auto it = resident.begin(); it != resident.end();) {
+        const std::shared_ptr<Job>& j = it->second;
+        if (--j->steps_left > 0) {
+          ++it;
+          continue;
+        }
+        j->pos.resize(3ull * j->n);
+        j->vel.resize(3ull * j->n);
+        j->dens.resize(2ull * j->n);
+        const int d = eng.Download(it->first, j->pos.data(), j->vel.data(), j->dens.data(),
+                                   false, stream);
+        eng.RemoveScene(it->first);
+        Finish(j, d, d == SPH_OK ? "" : eng.LastError());
+        it = resident.erase(it);
+      }
+    }
+  }
+};
+
+extern "C" {
+
+int sph_server_create(uint64_t budget_bytes, uint32_t max_scenes, int substeps,
+                      sph_server** out) {
+  if (!out || substeps < 1 || substeps > 64 || max_scenes == 0) return SPH_ERR_INVALID;
+  *out = nullptr;
+  const uint64_t cap = budget_bytes / sph::Engine::BytesPerParticle();
+  if (cap == 0) return SPH_ERR_INVALID;
+  std::unique_ptr<sph_server> s(new (std::nothrow) sph_server(cap, max_scenes, substeps));
+  if (!s) return SPH_ERR_NOMEM;
+  int rc = s->eng.Init();
+  if (rc != SPH_OK) return rc;
+  if (cudaGetDevice(&s->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return SPH_ERR_CUDA;
+  }
+  sph_server* raw = s.get();
+  raw->worker = std::thread([raw] { raw->Run(); });
+  *out = s.release();
+  return SPH_OK;
+}
+
+int sph_server_destroy(sph_server* s) {
+  if (!s) return SPH_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->work_cv.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return SPH_OK;
+}
+
+int sph_server_submit(sph_server* s, const sph_params* params, uint32_t n, const float* pos3,
+                      const float* vel3, float dt, uint32_t steps, uint64_t* job_id) {
+  if (!s || !params || !pos3 || !job_id || n == 0 || n >= (1u << 24) || steps == 0)
+    return SPH_ERR_INVALID;
+  if (n > s->eng.Capacity()) return SPH_ERR_NOMEM;  // could never be admitted
+  auto j = std::make_shared<Job>();
+  j->prm = *params;
+  j->n = n;
+  j->dt = dt;
+  j->steps_left = steps;
+  j->pos.assign(pos3, pos3 + 3ull * n);
+  if (vel3) j->vel.assign(vel3, vel3 + 3ull * n);
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    j->id = s->next_id++;
+    s->jobs[j->id] = j;
+    s->waiting.push_back(j);
+    ++s->submitted;
+  }
+  s->work_cv.notify_all();
+  *job_id = j->id;
+  return SPH_OK;
+}
+
+int sph_server_cancel(sph_server* s, uint64_t job_id) {
+  if (!s) return SPH_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(job_id);
+  if (it == s->jobs.end()) return SPH_ERR_INVALID;
+  const std::shared_ptr<Job>& j = it->second;
+  if (j->done) return SPH_OK;
+  j->cancel = true;
+  if (!j->resident) {
+    s->waiting.erase(std::remove(s->waiting.begin(), s->waiting.end(), j), s->waiting.end());
+    s->Finish(j, SPH_ERR_STATE, "cancelled");
+  }
+  // a resident job leaves the batch at the worker's next step boundary
+  return SPH_OK;
+}
+
+int sph_server_wait(sph_server* s, uint64_t job_id, float* pos3, float* vel3, float* dens2,
+                    double timeout_s) {
+  if (!s) return SPH_ERR_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(job_id);
+  if (it == s->jobs.end()) return SPH_ERR_INVALID;
+  std::shared_ptr<Job> j = it->second;
+  const auto limit = std::chrono::duration<double>(timeout_s < 0.0 ? 0.0 : timeout_s);
+  if (!s->done_cv.wait_for(lk, limit, [&] { return j->done; })) {
+    s->err = "job not finished within the timeout";
+    return SPH_ERR_STATE;
+  }
+  s->jobs.erase(job_id);
+  if (j->status != SPH_OK) {
+    s->err = j->why;
+    return j->status;
+  }
+  if (pos3) std::copy(j->pos.begin(), j->pos.end(), pos3);
+  if (vel3) std::copy(j->vel.begin(), j->vel.end(), vel3);
+  if (dens2) std::copy(j->dens.begin(), j->dens.end(), dens2);
+  return SPH_OK;
+}
+
+int sph_server_get_stats(sph_server* s, sph_server_stats* out) {
+  if (!s || !out) return SPH_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  *out = sph_server_stats{};
+  out->submitted = s->submitted;
+  out->completed = s->completed;
+  out->cancelled = s->cancelled;
+  out->failed = s->failed;
+  out->queued = static_cast<uint32_t>(s->waiting.size());
+  out->resident = static_cast<uint32_t>(s->resident.size());
+  out->steps = s->steps;
+  out->particle_steps = s->particle_steps;
+  out->capacity_particles = s->eng.Capacity();
+  if (s->started && s->steps) {
+    out->wall_s = Seconds(s->t_first, s->t_last);
+    out->particle_steps_per_s = out->wall_s > 0 ? s->particle_steps / out->wall_s : 0.0;
+    // per-step latency as the jobs see it: every step weighted by the jobs
+    // it advanced
+    std::vector<std::pair<float, uint32_t>> ms = s->step_ms;
+    std::sort(ms.begin(), ms.end());
+    uint64_t total = 0;
+    for (const auto& m : ms) total += m.second;
+    auto pct = [&](double q) {
+      const double want = q * static_cast<double>(total);
+      uint64_t acc = 0;
+      for (const auto& m : ms) {
+        acc += m.second;
+        if (static_cast<double>(acc) >= want) return static_cast<double>(m.first);
+      }
+      return static_cast<double>(ms.back().first);
+    };
+    out->p50_step_ms = pct(0.50);
+    out->p99_step_ms = pct(0.99);
+  }
+  return SPH_OK;
+}
+
+const char* sph_server_last_error(sph_server* s) {
+  if (!s) return "null server";
+  std::lock_guard<std::mutex> lk(s->mu);
+  thread_local std::string copy;
+  copy = s->err;
+  return copy.c_str();
+}
+
+}  // extern "C"

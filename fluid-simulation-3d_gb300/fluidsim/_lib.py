@@ -33,7 +33,9 @@ EXPORTS = (
     "sph_get_tuning", "sph_autotune", "sph_spatial_lookup_static",
     "sph_static_error", "sph_bytes_per_particle", "sph_batch_sync",
     "sph_render", "sph_batch_render", "sph_save", "sph_load", "sph_batch_save",
-    "sph_batch_add_snapshot",
+    "sph_batch_add_snapshot", "sph_server_create", "sph_server_destroy",
+    "sph_server_submit", "sph_server_cancel", "sph_server_wait", "sph_server_get_stats",
+    "sph_server_last_error",
 )
 STATIC_LOOKUP_MAX = 65536
 
@@ -69,6 +71,17 @@ class View(ctypes.Structure):
                 ("scale", ctypes.c_float), ("clear", ctypes.c_float * 4)]
 
 
+class ServerStats(ctypes.Structure):
+    """struct sph_server_stats."""
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("cancelled", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("queued", ctypes.c_uint32), ("resident", ctypes.c_uint32),
+                ("steps", ctypes.c_uint64), ("particle_steps", ctypes.c_uint64),
+                ("capacity_particles", ctypes.c_uint64), ("wall_s", ctypes.c_double),
+                ("particle_steps_per_s", ctypes.c_double),
+                ("p50_step_ms", ctypes.c_double), ("p99_step_ms", ctypes.c_double)]
+
+
 _P = ctypes.c_void_p
 _U32 = ctypes.c_uint32
 _lib = None
@@ -92,6 +105,13 @@ def _sig(L):
         "sph_out_positions": (i, [_P, ctypes.POINTER(_P)]),
         "sph_render": (i, [_P, ctypes.POINTER(View), _P, _P, _P]),
         "sph_batch_render": (i, [_P, u32, ctypes.POINTER(View), _P, _P, _P]),
+        "sph_server_create": (i, [u64, u32, i, ctypes.POINTER(_P)]),
+        "sph_server_destroy": (i, [_P]),
+        "sph_server_submit": (i, [_P, pp, u32, _P, _P, f, u32, ctypes.POINTER(u64)]),
+        "sph_server_cancel": (i, [_P, u64]),
+        "sph_server_wait": (i, [_P, u64, _P, _P, _P, ctypes.c_double]),
+        "sph_server_get_stats": (i, [_P, ctypes.POINTER(ServerStats)]),
+        "sph_server_last_error": (ctypes.c_char_p, [_P]),
         "sph_save": (i, [_P, ctypes.c_char_p, _P]),
         "sph_load": (i, [_P, ctypes.c_char_p, _P]),
         "sph_batch_save": (i, [_P, u32, ctypes.c_char_p, _P]),

@@ -268,3 +268,102 @@ def run_alone(req: Request, stream=None, tuning=None):
     out = sim.download()
     sim.close()
     return out
+
+
+class NativeServer:
+    """The library's own serving loop (sph_server_*): a worker thread in the
+    library admits jobs by the HBM budget, steps every resident job per
+    batched launch and retires finished ones; submit() returns at once and
+    wait() blocks for a job's result. Same admission rule and results as
+    Server, without Python in the loop."""
+
+    def __init__(self, budget_bytes: int, max_scenes: int = 4096, substeps: int = 3):
+        import ctypes
+        self._ct = ctypes
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        rc = self._lib.sph_server_create(int(budget_bytes), int(max_scenes), int(substeps),
+                                         ctypes.byref(h))
+        if rc != 0:
+            raise _lib.SphError(rc, (self._lib.sph_global_error() or b"").decode())
+        self._h = h
+        self.substeps = int(substeps)
+        self._sizes = {}
+
+    def _raise(self, rc):
+        msg = self._lib.sph_server_last_error(self._h) or b""
+        raise _lib.SphError(rc, msg.decode(errors="replace"))
+
+    def submit(self, params, pos, vel, dt, steps) -> int:
+        ct = self._ct
+        pos = np.ascontiguousarray(pos, np.float32)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32)
+        job = ct.c_uint64()
+        rc = self._lib.sph_server_submit(
+            self._h, ct.byref(to_params(params)), pos.shape[0], pos.ctypes.data,
+            None if v is None else v.ctypes.data, float(np.float32(dt)), int(steps),
+            ct.byref(job))
+        if rc != 0:
+            self._raise(rc)
+        self._sizes[job.value] = pos.shape[0]
+        return int(job.value)
+
+    def cancel(self, job: int) -> None:
+        rc = self._lib.sph_server_cancel(self._h, int(job))
+        if rc != 0:
+            self._raise(rc)
+
+    def wait(self, job: int, timeout: float = 600.0):
+        """(pos, vel, dens) of a finished job; SphError if it was cancelled,
+        failed or is still running after `timeout` seconds."""
+        n = self._sizes[int(job)]
+        pos = np.empty((n, 3), np.float32)
+        vel = np.empty((n, 3), np.float32)
+        dens = np.empty((n, 2), np.float32)
+        rc = self._lib.sph_server_wait(self._h, int(job), pos.ctypes.data, vel.ctypes.data,
+                                       dens.ctypes.data, float(timeout))
+        if rc != 0:
+            self._raise(rc)
+        self._sizes.pop(int(job), None)
+        return pos, vel, dens
+
+    def stats(self) -> dict:
+        s = _lib.ServerStats()
+        rc = self._lib.sph_server_get_stats(self._h, self._ct.byref(s))
+        if rc != 0:
+            self._raise(rc)
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def run(self, requests, realtime=True):
+        """Submit `requests` at their arrival times (all at once with
+        realtime=False) and collect every result: (results by rid, stats)."""
+        t0 = time.perf_counter()
+        jobs = {}
+        for r in sorted(requests, key=lambda q: q.arrival):
+            if realtime:
+                time.sleep(max(0.0, r.arrival - (time.perf_counter() - t0)))
+            if r.substeps != self.substeps:
+                raise ValueError("one substep count per server")
+            jobs[r.rid] = self.submit(r.params, r.pos, r.vel, r.dt, r.steps)
+        done = {}
+        for rid, job in jobs.items():
+            pos, vel, dens = self.wait(job)
+            done[rid] = Done(rid, pos, vel, dens, 0.0, time.perf_counter() - t0, [])
+        st = self.stats()
+        stats = dict(requests=len(done), batched_steps=st["steps"],
+                     particle_steps=st["particle_steps"], wall_s=st["wall_s"],
+                     particle_steps_per_s=st["particle_steps_per_s"],
+                     p50_step_ms=st["p50_step_ms"], p99_step_ms=st["p99_step_ms"],
+                     capacity_particles=st["capacity_particles"])
+        return done, stats
+
+    def close(self):
+        if self._h is not None:
+            self._lib.sph_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

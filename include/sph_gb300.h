@@ -303,6 +303,49 @@ int sph_batch_get_tuning(const sph_batch *b, sph_tuning *t);
 int sph_batch_autotune(sph_batch *b, int substeps, int steps_per_trial,
                        sph_tuning *best, float *best_ms, void *stream);
 
+/* Native serving loop (the served form): continuous batching of scene jobs
+ * on a worker thread over one batch engine whose capacity is
+ * budget_bytes / sph_bytes_per_particle(). Jobs are admitted in submission
+ * order while the budget has room (smaller later jobs may backfill); every
+ * resident job advances one step of dt (in `substeps` substeps, one count
+ * per server) per batched launch; a job leaves after its `steps` steps with
+ * its state read back. Results equal the job run alone, bit for bit.
+ * submit / cancel / wait / stats may be called from any thread; call
+ * destroy only when no other thread is inside a server call. */
+typedef struct sph_server sph_server;
+typedef struct sph_server_stats {
+  uint64_t submitted, completed, cancelled, failed;
+  uint32_t queued, resident;     /* jobs waiting / on the device now        */
+  uint64_t steps;                /* batched steps run                       */
+  uint64_t particle_steps;       /* sum over steps of resident particles    */
+  uint64_t capacity_particles;
+  double wall_s;                 /* first admission to the end of the last step */
+  double particle_steps_per_s;
+  double p50_step_ms, p99_step_ms; /* per-step wall clock as the jobs see it:
+                                    every step weighted by the jobs it
+                                    advanced                                 */
+} sph_server_stats;
+
+int sph_server_create(uint64_t budget_bytes, uint32_t max_scenes, int substeps,
+                      sph_server **out);
+int sph_server_destroy(sph_server *s);
+/* Copies the job's inputs (pos3, vel3 float[3n]; vel3 may be NULL); a job
+ * larger than the whole capacity is refused with SPH_ERR_NOMEM. */
+int sph_server_submit(sph_server *s, const sph_params *params, uint32_t n,
+                      const float *pos3, const float *vel3, float dt,
+                      uint32_t steps, uint64_t *job_id);
+/* A queued job is dropped at once, a resident one at the next step
+ * boundary; its wait returns SPH_ERR_STATE. */
+int sph_server_cancel(sph_server *s, uint64_t job_id);
+/* Blocks up to timeout_s for the job, then copies its result (host
+ * pointers, any may be NULL) and forgets it. SPH_ERR_STATE: still running
+ * after the timeout (wait again), or cancelled; other codes: the job
+ * failed (sph_server_last_error says why). */
+int sph_server_wait(sph_server *s, uint64_t job_id, float *pos3, float *vel3,
+                    float *dens2, double timeout_s);
+int sph_server_get_stats(sph_server *s, sph_server_stats *out);
+const char *sph_server_last_error(sph_server *s);
+
 /* Device bytes an engine allocates per particle of capacity (state, sort,
  * cell tables, neighbour lists): admission by an HBM budget divides by it. */
 uint64_t sph_bytes_per_particle(void);
