@@ -346,10 +346,26 @@ int Engine::Load(uint32_t id, const float* pos3, const float* vel3,
   const float* dv = vel3;
   const float* hp = device_ptrs ? nullptr : DeviceAlias(pos3);
   const float* hv = device_ptrs ? nullptr : DeviceAlias(vel3);
+  // A single scene whose device constants and layout are current (a step
+  // has run since the last change): the import also predicts the next
+  // step's first substep with those constants, and that step uses it if its
+  // dt and substeps are unchanged (the carry test in Step).
+  const bool predict = hp && (!vel3 || hv) && max_scenes_ == 1 && !scenes_dirty_ &&
+                       uploaded_substeps_ > 0 && !layout_dirty_ &&
+                       n_tiles_old_ == n_tiles_new_ && total_ == n;
   if (hp && (!vel3 || hv)) {
     // pinned host rows: the import kernel reads them over the link itself
-    SPH_CUDA(launch_import_rows(old_base_[id], n, hp, hv, d_pos_[cur_], d_vel_[cur_], st),
+    if (predict && count_extent_)
+      SPH_CUDA(cudaMemsetAsync(ctx_.count, 0, sizeof(uint32_t) * count_extent_, st),
+               "histogram reset");
+    SPH_CUDA(launch_import_rows(old_base_[id], n, hp, hv, d_pos_[cur_], d_vel_[cur_],
+                                predict ? ctx_.scenes + id : nullptr, ctx_.count,
+                                ctx_.keyrank, st),
              "import kernel");
+    if (predict) {
+      carry_valid_ = true;
+      count_extent_ = total_;
+    }
   } else if (!device_ptrs && pos3) {
     // Stage through the prediction / post-pressure buffers (rewritten by
     // every substep before use).

@@ -1024,10 +1024,14 @@ __global__ void k_import(uint32_t first, uint32_t n,
 constexpr int kXferBlock = 256;
 constexpr int kXferWarps = kXferBlock / 32;
 
+// With `scene` the kernel also predicts the next step's first substep for
+// the imported state exactly as k_predict_hash would (key, arrival rank,
+// cell, caller index, and the histogram), so that step can skip it.
 __global__ void __launch_bounds__(kXferBlock)
 k_import_rows(uint32_t first, uint32_t n, const float* __restrict__ ipos,
               const float* __restrict__ ivel, float4* __restrict__ pos,
-              float4* __restrict__ vel) {
+              float4* __restrict__ vel, const SceneDev* __restrict__ scene,
+              uint32_t* __restrict__ count, uint4* __restrict__ keyrank) {
   __shared__ __align__(16) float s_rows[kXferWarps][2][96];
   const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
   const uint32_t k0 = (blockIdx.x * kXferWarps + w) * 32u;
@@ -1051,12 +1055,21 @@ k_import_rows(uint32_t first, uint32_t n, const float* __restrict__ ipos,
     }
   }
   __syncwarp();
-  if (lane < cnt) {
-    const uint32_t k = k0 + lane;
-    pos[first + k] = make_float4(sp[3 * lane], sp[3 * lane + 1], sp[3 * lane + 2],
-                                 __uint_as_float(k));
-    vel[first + k] = ivel ? make_float4(sv[3 * lane], sv[3 * lane + 1], sv[3 * lane + 2], 0.0f)
-                          : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const bool live = lane < cnt;
+  const uint32_t k = k0 + lane;
+  float4 p4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), v4 = p4;
+  if (live) {
+    p4 = make_float4(sp[3 * lane], sp[3 * lane + 1], sp[3 * lane + 2], __uint_as_float(k));
+    if (ivel) v4 = make_float4(sv[3 * lane], sv[3 * lane + 1], sv[3 * lane + 2], 0.0f);
+    pos[first + k] = p4;
+    vel[first + k] = v4;
+  }
+  if (scene) {  // every lane of the warp takes part (warp-aggregated atomics)
+    const SceneDev S = *scene;
+    uint32_t key = 0, cell = 0;
+    if (live) predict_key(S, p4, v4, key, cell);
+    const uint32_t r = aggregated_rank(count, key, live);
+    if (live) keyrank[first + k] = make_uint4(key, r, cell, k);
   }
 }
 
@@ -1230,11 +1243,12 @@ cudaError_t launch_import(uint32_t first, uint32_t n, const float* ipos,
 
 cudaError_t launch_import_rows(uint32_t first, uint32_t n, const float* ipos,
                                const float* ivel, float4* pos, float4* vel,
+                               const SceneDev* scene, uint32_t* count, uint4* keyrank,
                                cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const uint32_t warps = (n + 31) / 32;
   k_import_rows<<<(warps + kXferWarps - 1) / kXferWarps, kXferBlock, 0, st>>>(
-      first, n, ipos, ivel, pos, vel);
+      first, n, ipos, ivel, pos, vel, scene, count, keyrank);
   return cudaGetLastError();
 }
 

@@ -130,9 +130,12 @@ cudaError_t launch_import(uint32_t first, uint32_t n, const float* ipos,
                           const float* ivel, float4* pos, float4* vel,
                           cudaStream_t st);
 // The same import reading host memory the device addresses directly (pinned
-// buffers, 16-byte aligned): rows move as aligned float4 per warp.
+// buffers, 16-byte aligned): rows move as aligned float4 per warp. With
+// `scene` (the scene's device constants) it also writes the next step's
+// first prediction (keyrank, histogram in count) as k_predict_hash does.
 cudaError_t launch_import_rows(uint32_t first, uint32_t n, const float* ipos,
                                const float* ivel, float4* pos, float4* vel,
+                               const SceneDev* scene, uint32_t* count, uint4* keyrank,
                                cudaStream_t st);
 
 }  // namespace sph

@@ -108,3 +108,39 @@ def test_pinned_download_subsets(gpu_lib):
     finally:
         pin.free()
         sim.close()
+
+
+def test_pinned_upload_prediction_follows_dt_and_substeps(gpu_lib):
+    """A pinned upload into a handle that has stepped predicts the next step
+    with its last dt and substeps; a step with another dt or substep count
+    must discard that prediction. Pinned and pageable uploads give the same
+    bits through a sequence that changes both."""
+    import fluidsim
+    from fluidsim import scenes
+    sc = scenes.batched_scenes(count=1, seed=19, lo=3000, hi=3000)[0]
+    n = sc["pos"].shape[0]
+    plan = [(sc["dt"], 3), (sc["dt"], 3), (sc["dt"] * 0.5, 3), (sc["dt"] * 0.5, 2),
+            (sc["dt"] * 0.5, 2), (sc["dt"], 3)]
+
+    def run(make):
+        sim = fluidsim.FluidSimulation(sc["params"])
+        sim.InitializeData(n, sc["pos"], sc["vel"])
+        lib, h = sim._lib, sim.handle
+        pos, vel = make((n, 3)), make((n, 3))
+        pos[:] = sc["pos"]
+        vel[:] = sc["vel"]
+        for dt, ss in plan:
+            assert lib.sph_upload(h, pos.ctypes.data, vel.ctypes.data, sim._stream) == 0
+            sim.step_async(dt, ss)
+            assert lib.sph_download(h, pos.ctypes.data, vel.ctypes.data, None, sim._stream) == 0
+        assert sim.status() == 0
+        sim.close()
+        return pos.copy(), vel.copy()
+
+    pin = Pinned()
+    try:
+        got = run(lambda shape: pin.array(shape))
+    finally:
+        pin.free()
+    want = run(lambda shape: np.empty(shape, np.float32))
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
