@@ -111,6 +111,7 @@ struct sph_server {
       } else {
         j->scene = sid;
         j->resident = true;
+        std::vector<float>().swap(j->pos);  // on the device now; results reuse them
         std::vector<float>().swap(j->vel);
         resident[sid] = j;
         if (!started) {
