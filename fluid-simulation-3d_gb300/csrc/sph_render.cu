@@ -19,8 +19,8 @@
 //  - pixel centres (px + 1/2, py + 1/2) inside [X0, X1) x (Y0, Y1] (GL's
 //    top-left rule in its y-up window coordinates);
 //  - the offset at a pixel centre is linear across the quad: v = f (2 o) - o
-//    with f the centre's fraction of the quad; discard if
-//    sqrt(vx^2 + vy^2) > s / 4;
+//    with f = (centre - X0) * (1 / (X1 - X0)) the centre's fraction of the
+//    quad; discard if vx^2 + vy^2 > (s / 4)^2;
 //  - the nearest fragment wins, ties to the lower particle index (first
 //    drawn under GL_LESS), through a 64-bit atomicMin of (depth bits,
 //    caller index): deterministic whatever the launch order;
@@ -82,25 +82,22 @@ __device__ __forceinline__ float row_dot(const float* m, int r, float x, float y
   return fa(fa(fm(m[r], x), fm(m[4 + r], y)), fa(fm(m[8 + r], z), m[12 + r]));
 }
 
-// Pixels of one splat from row ya, column xa, in a (xb - xa + 1)-wide box,
-// visited from index `start` with stride `step`: the discard test and the
-// depth test of particleRender.fs for each pixel centre.
-__device__ __forceinline__ void splat_pixels(const RenderView& v, int xa, int xb, int ya, int yb,
-                                             float x0, float x1, float y0, float y1,
-                                             unsigned long long key, int start, int step,
-                                             unsigned long long* __restrict__ keys) {
-  const float dx = fs(x1, x0), dy = fs(y1, y0);
-  const float two_ox = fa(v.ox, v.ox), two_oy = fa(v.oy, v.oy);
-  const int w = xb - xa + 1, area = w * (yb - ya + 1);
-  for (int t = start; t < area; t += step) {
-    const int py = ya + t / w, px = xa + t % w;
-    const float fy = fd(fs(fa(static_cast<float>(py), 0.5f), y0), dy);
-    const float vy = fs(fm(fy, two_oy), v.oy);
-    const float fx = fd(fs(fa(static_cast<float>(px), 0.5f), x0), dx);
-    const float vx = fs(fm(fx, two_ox), v.ox);
-    if (__fsqrt_rn(fa(fm(vx, vx), fm(vy, vy))) > v.q) continue;  // discard
-    atomicMin(keys + static_cast<uint64_t>(py) * v.width + px, key);
-  }
+// The discard and depth tests of particleRender.fs at the centre of pixel
+// (px, py) of a splat whose quad spans [x0, x1) x (y0, y1] in window
+// coordinates (idx, idy: the reciprocal widths).
+__device__ __forceinline__ void splat_pixel(const RenderView& v, int px, float vy2, float x0,
+                                            float idx, float q2, unsigned long long key,
+                                            unsigned long long* __restrict__ row) {
+  const float fx = fm(fs(fa(static_cast<float>(px), 0.5f), x0), idx);
+  const float vx = fs(fm(fx, fa(v.ox, v.ox)), v.ox);
+  if (fa(fm(vx, vx), vy2) > q2) return;  // discard: |offset| > s/4
+  atomicMin(row + px, key);
+}
+
+__device__ __forceinline__ float splat_vy2(const RenderView& v, int py, float y0, float idy) {
+  const float fy = fm(fs(fa(static_cast<float>(py), 0.5f), y0), idy);
+  const float vy = fs(fm(fy, fa(v.oy, v.oy)), v.oy);
+  return fm(vy, vy);
 }
 
 // Particles of the scene's slots [first, first + n), one per thread: its
@@ -160,8 +157,16 @@ __global__ void k_splat(uint32_t first, uint32_t n, const float4* __restrict__ p
   }
   const unsigned long long key =
       (static_cast<unsigned long long>(__float_as_uint(depth)) << 32) | id;
+  const float q2 = fm(v.q, v.q);
   const bool big = live && (xb - xa + 1) * (yb - ya + 1) > kWarpSplat;
-  if (live && !big) splat_pixels(v, xa, xb, ya, yb, x0, x1, y0, y1, key, 0, 1, keys);
+  if (live && !big) {
+    const float idx = fd(1.0f, fs(x1, x0)), idy = fd(1.0f, fs(y1, y0));
+    for (int py = ya; py <= yb; ++py) {
+      const float vy2 = splat_vy2(v, py, y0, idy);
+      unsigned long long* row = keys + static_cast<uint64_t>(py) * v.width;
+      for (int px = xa; px <= xb; ++px) splat_pixel(v, px, vy2, x0, idx, q2, key, row);
+    }
+  }
   // large splats, one at a time across the warp (every lane arrives here)
   for (uint32_t m = __ballot_sync(0xffffffffu, big); m; m &= m - 1u) {
     const int src = __ffs(m) - 1;
@@ -172,8 +177,13 @@ __global__ void k_splat(uint32_t first, uint32_t n, const float4* __restrict__ p
     const uint32_t klo = __shfl_sync(0xffffffffu, static_cast<uint32_t>(key), src);
     const uint32_t khi = __shfl_sync(0xffffffffu, static_cast<uint32_t>(key >> 32), src);
     const unsigned long long bkey = (static_cast<unsigned long long>(khi) << 32) | klo;
-    splat_pixels(v, bxa, bxb, bya, byb, bx0, bx1, by0, by1, bkey, static_cast<int>(lane), 32,
-                 keys);
+    const float idx = fd(1.0f, fs(bx1, bx0)), idy = fd(1.0f, fs(by1, by0));
+    const int w = bxb - bxa + 1, area = w * (byb - bya + 1);
+    for (int t = static_cast<int>(lane); t < area; t += 32) {
+      const int py = bya + t / w;
+      splat_pixel(v, bxa + t % w, splat_vy2(v, py, by0, idy), bx0, idx, q2, bkey,
+                  keys + static_cast<uint64_t>(py) * v.width);
+    }
   }
 }
 

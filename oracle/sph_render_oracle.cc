@@ -100,19 +100,20 @@ int sph_oracle_render(const float* pos3, const float* vel3, uint32_t n, const fl
     const int xa = std::max(px0, 0), xb = std::min(px1, static_cast<int>(width) - 1);
     const int ya = std::max(py0, 0), yb = std::min(py1, static_cast<int>(height) - 1);
     if (xa > xb || ya > yb) continue;
-    const float dx = x1 - x0, dy = y1 - y0;
+    const float idx = 1.0f / (x1 - x0), idy = 1.0f / (y1 - y0);
     const float two_ox = ox + ox, two_oy = oy + oy;
+    const float q2 = q * q;
     uint32_t dbits;
     std::memcpy(&dbits, &dep, 4);
     const uint64_t key = (static_cast<uint64_t>(dbits) << 32) | id;
     for (int py = ya; py <= yb; ++py) {
-      const float fy = ((static_cast<float>(py) + 0.5f) - y0) / dy;
+      const float fy = ((static_cast<float>(py) + 0.5f) - y0) * idy;
       const float vyy = fy * two_oy - oy;
       const float vy2 = vyy * vyy;
       for (int px = xa; px <= xb; ++px) {
-        const float fx = ((static_cast<float>(px) + 0.5f) - x0) / dx;
+        const float fx = ((static_cast<float>(px) + 0.5f) - x0) * idx;
         const float vxx = fx * two_ox - ox;
-        if (std::sqrt(vxx * vxx + vy2) > q) continue;
+        if (vxx * vxx + vy2 > q2) continue;  // discard: |offset| > s/4
         uint64_t& k = keys[static_cast<uint64_t>(py) * width + px];
         if (key < k) k = key;
       }
