@@ -10,6 +10,7 @@
 // as a single-scene step.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -43,6 +44,36 @@ double Seconds(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double>(b - a).count();
 }
 
+// Step latencies in a fixed log-spaced histogram, so a long-running server
+// keeps constant memory: bin b holds [1 us * kRatio^b, 1 us * kRatio^(b+1)),
+// 0.5% wide, up to about 1,000 s; a percentile reports its bin's geometric
+// centre (within 0.25% of the step time it stands for).
+struct LatencyHistogram {
+  static constexpr int kBins = 4200;
+  static constexpr double kRatio = 1.005;
+  static constexpr double kLowMs = 1e-3;
+  std::vector<uint64_t> weight = std::vector<uint64_t>(kBins, 0);
+  uint64_t total = 0;
+
+  void Add(double ms, uint32_t w) {
+    int b = 0;
+    if (ms > kLowMs) b = static_cast<int>(std::log(ms / kLowMs) / std::log(kRatio));
+    weight[std::min(std::max(b, 0), kBins - 1)] += w;
+    total += w;
+  }
+  // the smallest bin centre at or below which a fraction q of the weight lies
+  double Percentile(double q) const {
+    const double want = q * static_cast<double>(total);
+    uint64_t acc = 0;
+    int b = 0;
+    for (; b < kBins - 1; ++b) {
+      acc += weight[b];
+      if (weight[b] && static_cast<double>(acc) >= want) break;
+    }
+    return kLowMs * std::pow(kRatio, b + 0.5);
+  }
+};
+
 }  // namespace
 
 struct sph_server {
@@ -61,7 +92,7 @@ struct sph_server {
   // statistics (under mu)
   uint64_t submitted = 0, completed = 0, cancelled = 0, failed = 0;
   uint64_t steps = 0, particle_steps = 0;
-  std::vector<std::pair<float, uint32_t>> step_ms;  // (ms, jobs it advanced)
+  LatencyHistogram step_ms;  // each step weighted by the jobs it advanced
   bool started = false;
   Clock::time_point t_first{}, t_last{};
   std::string err;
@@ -162,7 +193,7 @@ struct sph_server {
       }
       ++steps;
       particle_steps += live;
-      step_ms.emplace_back(static_cast<float>(1000.0 * Seconds(t0, t1)), nres);
+      step_ms.Add(1000.0 * Seconds(t0, t1), nres);
       t_last = t1;
       for (auto it = resident.begin(); it != resident.end();) {
         const std::shared_ptr<Job>& j = it->second;
@@ -300,21 +331,8 @@ int sph_server_get_stats(sph_server* s, sph_server_stats* out) {
     out->particle_steps_per_s = out->wall_s > 0 ? s->particle_steps / out->wall_s : 0.0;
     // per-step latency as the jobs see it: every step weighted by the jobs
     // it advanced
-    std::vector<std::pair<float, uint32_t>> ms = s->step_ms;
-    std::sort(ms.begin(), ms.end());
-    uint64_t total = 0;
-    for (const auto& m : ms) total += m.second;
-    auto pct = [&](double q) {
-      const double want = q * static_cast<double>(total);
-      uint64_t acc = 0;
-      for (const auto& m : ms) {
-        acc += m.second;
-        if (static_cast<double>(acc) >= want) return static_cast<double>(m.first);
-      }
-      return static_cast<double>(ms.back().first);
-    };
-    out->p50_step_ms = pct(0.50);
-    out->p99_step_ms = pct(0.99);
+    out->p50_step_ms = s->step_ms.Percentile(0.50);
+    out->p99_step_ms = s->step_ms.Percentile(0.99);
   }
   return SPH_OK;
 }
