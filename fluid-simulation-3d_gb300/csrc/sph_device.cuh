@@ -44,10 +44,14 @@ constexpr int kTile = 32;
 
 // Per-scene descriptor, built on the host from sph_params.
 struct SceneDev {
-  uint32_t n;         // particles (and key-table size: key = index % n)
-  uint32_t base;      // first slot of the scene's current layout / table
+  uint32_t n;         // particles
+  uint32_t base;      // first slot of the scene's current layout
   uint64_t fm;        // Lemire magic for x % n
+  uint32_t tbase;     // first entry of the scene's key table
+  uint32_t direct;    // 1: one key per grid cell (key = cell index, the grid
+                      //    clamped); 0: n keys, key = cell index % n
   uint32_t gx0, gy0, gz0;  // origin cell of the internal grid (int32 bits)
+  uint32_t gnx, gny, gnz;  // grid cells per axis
   uint32_t gwy, gwz;  // y and z strides of the internal cell index
   float r;            // interaction radius
   float cut_lt;       // d2 <= cut_lt  <=>  d2 <= sqrRadius && sqrtf(d2) < r
@@ -104,16 +108,39 @@ __device__ __forceinline__ uint32_t hash_of(const SceneDev& S, float3 pr) {
   return hash_cell(cell_of(pr.x, S.r), cell_of(pr.y, S.r), cell_of(pr.z, S.r));
 }
 
+// Grid coordinate of cell c along one axis, clamped to [1, count - 2]: the
+// grid's first and last cells stay empty, so the three x-neighbours of any
+// occupied cell are consecutive indices of one row. Clamping is monotone, so
+// cells that are neighbours stay neighbours (a cell beyond the grid shares
+// the edge cell with the cells between, and the cutoff test drops the extra
+// candidates this brings).
+// (The origin lies in [-1e9, 1e9] and count in [5, 2^15], so the bounds fit
+// an int.)
+__device__ __forceinline__ uint32_t grid_coord(int c, uint32_t origin, uint32_t count) {
+  const int lo = static_cast<int>(origin) + 1;
+  const int hi = lo + static_cast<int>(count) - 3;
+  return static_cast<uint32_t>(min(max(c, lo), hi) - lo) + 1u;
+}
+
 // Internal cell index of the sort (the reference's cells, another key):
-// (cx - x0) + (cy - y0) * wy + (cz - z0) * wz modulo 2^32. Linear in the
-// wrapped cell coordinates like HashCell, so index(c + d) = index(c) + dx +
-// dy*wy + dz*wz for every cell, and distinct neighbour offsets never share
-// an index (|dx + dy*wy + dz*wz| < 2^32).
+// (cx - x0) + (cy - y0) * wy + (cz - z0) * wz, with the coordinates clamped
+// to the grid for a direct table, else modulo 2^32. Linear in the cell
+// coordinates like HashCell, so index(c + d) = index(c) + dx + dy*wy + dz*wz
+// for every occupied cell, and distinct neighbour offsets never share an
+// index (|dx + dy*wy + dz*wz| < 2^32).
 __device__ __forceinline__ uint32_t cell_index(const SceneDev& S, float3 pr) {
-  const uint32_t cx = static_cast<uint32_t>(cell_of(pr.x, S.r)) - S.gx0;
-  const uint32_t cy = static_cast<uint32_t>(cell_of(pr.y, S.r)) - S.gy0;
-  const uint32_t cz = static_cast<uint32_t>(cell_of(pr.z, S.r)) - S.gz0;
-  return cx + cy * S.gwy + cz * S.gwz;
+  const int x = cell_of(pr.x, S.r), y = cell_of(pr.y, S.r), z = cell_of(pr.z, S.r);
+  if (S.direct)
+    return grid_coord(x, S.gx0, S.gnx) + grid_coord(y, S.gy0, S.gny) * S.gwy +
+           grid_coord(z, S.gz0, S.gnz) * S.gwz;
+  return (static_cast<uint32_t>(x) - S.gx0) + (static_cast<uint32_t>(y) - S.gy0) * S.gwy +
+         (static_cast<uint32_t>(z) - S.gz0) * S.gwz;
+}
+
+// Key-table entry of a cell: its own entry in a direct table, else its
+// bucket, cell index mod n (a bucket may then hold several cells).
+__device__ __forceinline__ uint32_t table_key(const SceneDev& S, uint32_t cell) {
+  return S.tbase + (S.direct ? cell : fastmod(cell, S.fm, S.n));
 }
 
 // Run-length flag of a cell-table row whose three x-runs are one contiguous

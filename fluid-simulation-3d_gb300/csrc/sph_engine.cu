@@ -64,19 +64,33 @@ uint32_t GridAxis(float h, float r, uint32_t* origin) {
   return static_cast<uint32_t>(std::min(hi - lo + 1.0, 32768.0));
 }
 
-SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base,
+// The key table of a scene: one entry per grid cell (a direct table, where a
+// cell's run needs no bucket search) when the grid has at most two cells per
+// particle, else n entries holding cell index mod n. The choice depends on
+// the scene alone, so a scene steps bit for bit alike in any batch. The
+// table buffers hold kTablePerParticle entries per particle of capacity plus
+// an allowance that tuning.table = 2 spends on direct tables for scenes with
+// larger grids.
+constexpr uint64_t kDirectCellsPerParticle = 2;
+constexpr uint64_t kTablePerParticle = kDirectCellsPerParticle;
+constexpr uint64_t kTableAllowance = 65536;
+
+// The scene's constants with a bucket table at `tbase`; the caller switches
+// to a direct table (direct = 1) where it has room for one.
+SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base, uint32_t tbase,
                       float sub_dt) {
   SceneDev d{};
   d.n = n;
   d.base = base;
+  d.tbase = tbase;
   d.fm = (~static_cast<uint64_t>(0)) / n + 1;
   const float r = p.radius;
   d.r = r;
-  const uint32_t gx = GridAxis(p.bound[0] * 0.5f, r, &d.gx0);
-  const uint32_t gy = GridAxis(p.bound[1] * 0.5f, r, &d.gy0);
-  GridAxis(p.bound[2] * 0.5f, r, &d.gz0);
-  d.gwy = gx;
-  d.gwz = gx * gy;  // modulo 2^32
+  d.gnx = GridAxis(p.bound[0] * 0.5f, r, &d.gx0);
+  d.gny = GridAxis(p.bound[1] * 0.5f, r, &d.gy0);
+  d.gnz = GridAxis(p.bound[2] * 0.5f, r, &d.gz0);
+  d.gwy = d.gnx;
+  d.gwz = d.gnx * d.gny;  // modulo 2^32
   const float t_lt = LargestWith(r, [r](float s) { return s < r; });
   const float t_le = LargestWith(r, [r](float s) { return s <= r; });
   d.cut_lt = std::min(p.cutoff_sq, t_lt);
@@ -101,6 +115,10 @@ SceneDev MakeSceneDev(const sph_params& p, uint32_t n, uint32_t base,
   d.pdt = p.predict_dt;
   d.dt = sub_dt;
   return d;
+}
+
+uint64_t GridCells(const SceneDev& d) {
+  return static_cast<uint64_t>(d.gnx) * d.gny * d.gnz;
 }
 
 template <class T> cudaError_t Alloc(T** p, uint64_t count) {
@@ -154,9 +172,12 @@ int Engine::CudaFail(cudaError_t e, const char* what) {
   } while (0)
 
 int Engine::Init() {
-  if (capacity_ == 0 || capacity_ >= (1ull << 31) || max_scenes_ == 0 ||
+  // (the key table, 2 entries a particle plus the allowance, is indexed by
+  // 32-bit keys)
+  if (capacity_ == 0 || capacity_ >= (1ull << 31) - kTableAllowance || max_scenes_ == 0 ||
       max_scenes_ >= (1u << kTileSceneBits))
-    return Fail(SPH_ERR_INVALID, "capacity must be in [1, 2^31) and scenes in [1, 2^27)");
+    return Fail(SPH_ERR_INVALID,
+                "capacity must be in [1, 2^31 - 2^16) and scenes in [1, 2^27)");
   int dev = 0;
   SPH_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
   SPH_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, dev),
@@ -190,9 +211,10 @@ int Engine::Init() {
   chk(Alloc(&ctx_.cell_first, C));
   chk(Alloc(&ctx_.cell_tab, C * 27ull));
   chk(Alloc(&ctx_.nbr, C * static_cast<uint64_t>(kNbrCap)));
-  chk(Alloc(&ctx_.count, C));
-  chk(Alloc(&ctx_.start, C + 1));
-  chk(Alloc(&ctx_.partial, scan_partials_needed(C)));
+  const uint64_t T = kTablePerParticle * C + kTableAllowance;  // key-table entries
+  chk(Alloc(&ctx_.count, T));
+  chk(Alloc(&ctx_.start, T + 1));
+  chk(Alloc(&ctx_.partial, scan_partials_needed(T)));
   chk(Alloc(&d_out4_, C));
   chk(Alloc(&d_status_, 1));
   if (e != cudaSuccess) {
@@ -201,7 +223,7 @@ int Engine::Init() {
                ? Fail(SPH_ERR_NOMEM, "device allocation failed")
                : CudaFail(e, "cudaMalloc");
   }
-  SPH_CUDA(cudaMemset(ctx_.count, 0, C * sizeof(uint32_t)), "cudaMemset");
+  SPH_CUDA(cudaMemset(ctx_.count, 0, T * sizeof(uint32_t)), "cudaMemset");
   SPH_CUDA(cudaMemset(ctx_.dens_a, 0, C * sizeof(float2)), "cudaMemset");
   SPH_CUDA(cudaMemset(d_status_, 0, sizeof(uint32_t)), "cudaMemset");
   SPH_CUDA(cudaMemset(d_out4_, 0, C * sizeof(float4)), "cudaMemset");
@@ -222,7 +244,7 @@ uint64_t Engine::BytesPerParticle() {
                                                  // cell_first, ncount
          + 27 * sizeof(uint2)                  // cell_tab
          + kNbrCap * sizeof(uint32_t)          // nbr
-         + 2 * sizeof(uint32_t)                // count, start
+         + kTablePerParticle * 2 * sizeof(uint32_t)  // count, start
          + sizeof(float4)                      // out4
          + sizeof(uint2);                      // tiles (old + new, per 32)
 }
@@ -364,7 +386,7 @@ int Engine::Load(uint32_t id, const float* pos3, const float* vel3,
              "import kernel");
     if (predict) {
       carry_valid_ = true;
-      count_extent_ = total_;
+      count_extent_ = table_total_;
     }
   } else if (!device_ptrs && pos3) {
     // Stage through the prediction / post-pressure buffers (rewritten by
@@ -434,11 +456,36 @@ int Engine::UploadScenes(int substeps, cudaStream_t st) {
   if (!scenes_dirty_ && uploaded_substeps_ == substeps) return SPH_OK;
   std::vector<SceneDev> h(max_scenes_);
   uint32_t hi = 0;
+  uint64_t tb = 0;  // key tables in layout order, like the slots
+  uint64_t allowance = kTableAllowance;
+  uint32_t n_direct = 0, n_live = 0;
   for (uint32_t s = 0; s < max_scenes_; ++s) {
     const Scene& sc = scenes_[s];
     if (!sc.live) continue;
-    h[s] = MakeSceneDev(sc.prm, sc.n, sc.base, sc.dt / static_cast<float>(substeps));
+    SceneDev& d = h[s];
+    d = MakeSceneDev(sc.prm, sc.n, sc.base, static_cast<uint32_t>(tb),
+                     sc.dt / static_cast<float>(substeps));
+    const uint64_t cells = GridCells(d);
+    if (tuning_.table != 1 && cells <= kDirectCellsPerParticle * sc.n) {
+      d.direct = 1;
+    } else if (tuning_.table == 2 && cells - sc.n <= allowance) {
+      d.direct = 1;
+      allowance -= cells - sc.n;
+    }
+    tb += d.direct ? cells : sc.n;
+    n_direct += d.direct;
+    ++n_live;
     hi = s + 1;
+  }
+  const int tables = n_direct == n_live ? kTablesDirect
+                     : n_direct == 0    ? kTablesBuckets
+                                        : kTablesMixed;
+  if (tb != table_total_ || tables != tables_) {
+    // the scan's length and the kernels' table forms are part of the
+    // captured graphs
+    table_total_ = static_cast<uint32_t>(tb);
+    tables_ = tables;
+    ReleaseGraphs();
   }
   if (hi)
     SPH_CUDA(cudaMemcpyAsync(d_scenes_, h.data(), sizeof(SceneDev) * hi,
@@ -457,6 +504,7 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st, bool carry) {
   c.block_force = tuning_.force_block ? tuning_.force_block : tuning_.block;
   c.cell_tile = tuning_.cell_tile;
   c.gather = tuning_.gather;
+  c.tables = tables_;
   c.pdl = !profile_;  // phase events between kernels need plain launches
   c.max_blocks = 0;
   c.src_limit = static_cast<uint32_t>(capacity_);
@@ -487,7 +535,7 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st, bool carry) {
     mark(0);
     if (ss == 0 && !carry) e = launch_predict_hash(c, first, st);
     mark(1);
-    if (e == cudaSuccess) e = launch_scan(c, total_, st);
+    if (e == cudaSuccess) e = launch_scan(c, table_total_, st);
     if (e == cudaSuccess) e = launch_sort_reorder(c, first, tnew, total_, st);
     mark(2);
     if (e == cudaSuccess && dbg) e = launch_ref_lookup(c, tnew, total_, st);
@@ -600,9 +648,9 @@ int Engine::Step(int substeps, cudaStream_t st) {
     SPH_CUDA(cudaEventRecord(join_out_, work_), "cudaEventRecord");
     SPH_CUDA(cudaStreamWaitEvent(st, join_out_, 0), "cudaStreamWaitEvent");
     launches_ += static_cast<uint64_t>(carry ? 0 : kKernelsPredict) +
-                 static_cast<uint64_t>(kernels_per_substep(total_)) * substeps;
+                 static_cast<uint64_t>(kernels_per_substep(table_total_, tables_)) * substeps;
     carry_valid_ = true;
-    count_extent_ = total_;
+    count_extent_ = table_total_;
     profiled_substeps_ = profile_ ? substeps : 0;
     if (substeps & 1) cur_ = 1 - cur_;
   }
@@ -829,10 +877,13 @@ int Engine::SetTuning(const sph_tuning& t) {
   if (t.force_block != 0 &&
       (t.force_block < 32 || t.force_block > 1024 || (t.force_block & 31)))
     return Fail(SPH_ERR_INVALID, "force_block must be 0 or a multiple of 32 in [32, 1024]");
+  if (t.table < 0 || t.table > 2)
+    return Fail(SPH_ERR_INVALID, "table must be 0 (automatic), 1 (buckets) or 2 (grid)");
   if (t.block != tuning_.block || t.particles_per_warp != tuning_.particles_per_warp ||
       t.cell_tile != tuning_.cell_tile || t.gather != tuning_.gather ||
       t.force_block != tuning_.force_block)
     ReleaseGraphs();
+  if (t.table != tuning_.table) scenes_dirty_ = true;  // new keys and tables
   tuning_ = t;
   return SPH_OK;
 }
@@ -875,13 +926,13 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
     if (round == 0) {
       for (int b : {64, 128, 256, 512})
         for (int tile : {1, 64, 128, 256})
-          space.push_back(sph_tuning{b, tile, 32, tuning_.gather, 0});
+          space.push_back(sph_tuning{b, tile, 32, tuning_.gather, 0, tuning_.table});
     } else if (round == 1) {
       for (int fb : {64, 128, 256, 512})
-        space.push_back(sph_tuning{win.block, win.cell_tile, 32, win.gather, fb});
+        space.push_back(sph_tuning{win.block, win.cell_tile, 32, win.gather, fb, win.table});
     } else {
       for (int g : {2, 4, 8})
-        space.push_back(sph_tuning{win.block, win.cell_tile, 32, g, win.force_block});
+        space.push_back(sph_tuning{win.block, win.cell_tile, 32, g, win.force_block, win.table});
     }
     for (const sph_tuning& t : space) {
       if ((rc = SetTuning(t)) != SPH_OK) break;

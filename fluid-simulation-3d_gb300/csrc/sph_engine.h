@@ -108,7 +108,9 @@ class Engine {
   // the first one that fits before it appends past the layout's end, so the
   // room a removed scene leaves is usable before the next step.
   std::vector<std::pair<uint64_t, uint64_t>> free_;
-  uint32_t total_ = 0;              // live particles (table length)
+  uint32_t total_ = 0;              // live particles
+  uint32_t table_total_ = 0;        // key-table entries of the live scenes
+  int tables_ = kTablesMixed;       // their forms (TableForms)
   bool layout_dirty_ = true;
   bool scenes_dirty_ = true;
   int uploaded_substeps_ = -1;
@@ -158,7 +160,7 @@ class Engine {
   // Neighbour-list capacity per particle (pairs with dist <= r); a particle
   // with more neighbours is handled by the bucket walk in the force passes.
   static constexpr uint32_t kNbrCap = 64;
-  sph_tuning tuning_{128, 1, 32, 4, 0};
+  sph_tuning tuning_{128, 1, 32, 4, 0, 0};
   int sm_count_ = 0;
 
   // The substep pipeline runs on an engine-owned non-blocking stream (stream

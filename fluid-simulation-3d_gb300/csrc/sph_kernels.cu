@@ -139,19 +139,40 @@ __device__ __forceinline__ uint32_t aggregated_rank(uint32_t* count,
   return base + __popc(peers & ((1u << lane) - 1u));
 }
 
-// Neighbour walk of a particle through its cell's table (k_cell_table): the
-// particles of the 27 neighbour cells -- every candidate the reference's
-// bucket loops would accept within the cutoff -- row by row, a merged row as
-// one run.
-template <class F>
-__device__ __forceinline__ void walk_runs(const uint2* __restrict__ cell_tab,
-                                          uint32_t cf,
+// Row w (dy = w/3 - 1, dz = w%3 - 1) of a cell of a direct key table: its
+// three x-neighbour cells are consecutive table entries, so the row is one
+// run from two start-table reads. k0 = tbase + cell - gwy - gwz, the entry of
+// row 0's middle cell.
+__device__ __forceinline__ uint2 direct_row(const SceneDev& S,
+                                            const uint32_t* __restrict__ start,
+                                            uint32_t k0, int w) {
+  const uint32_t k = k0 + static_cast<uint32_t>(w / 3) * S.gwy +
+                     static_cast<uint32_t>(w % 3) * S.gwz;
+  const uint32_t f = __ldg(start + k - 1);
+  return make_uint2(f, (__ldg(start + k + 2) - f) | kRunMerged);
+}
+
+// Neighbour walk of a particle: the particles of its cell's 27 neighbour
+// cells -- every candidate the reference's bucket loops would accept within
+// the cutoff -- row by row, a merged row as one run. A direct key table
+// gives each row from the start table (cell = the particle's cell index);
+// otherwise the rows come from the cell's table built by k_cell_table (cf =
+// the cell's first slot). Both visit the same particles in the same order.
+template <int kTables, class F>
+__device__ __forceinline__ void walk_runs(const SceneDev& S,
+                                          const uint32_t* __restrict__ start,
+                                          const uint2* __restrict__ cell_tab,
+                                          uint32_t cf, uint32_t cell,
                                           const float4* __restrict__ pred,
                                           F&& visit) {
-  const uint2* row = cell_tab + static_cast<uint64_t>(cf) * 27u;
+  const bool direct = kTables == kTablesDirect    ? true
+                    : kTables == kTablesBuckets ? false
+                                                : S.direct != 0u;
+  const uint2* row = cell_tab + static_cast<uint64_t>(direct ? 0u : cf) * 27u;
+  const uint32_t k0 = S.tbase + cell - S.gwy - S.gwz;
 #pragma unroll 1
   for (int w = 0; w < 9; ++w, row += 3) {
-    const uint2 m = __ldg(row);
+    const uint2 m = direct ? direct_row(S, start, k0, w) : __ldg(row);
     if (m.y & kRunMerged) {
       const uint32_t e = m.x + (m.y & ~kRunMerged);
 #pragma unroll 1
@@ -174,7 +195,7 @@ __device__ __forceinline__ void predict_key(const SceneDev& S, float4 p,
   float3 vn, pr;
   predict(S, p, v, vn, pr);
   cell = cell_index(S, pr);
-  key = S.base + fastmod(cell, S.fm, S.n);
+  key = table_key(S, cell);
 }
 
 __global__ void k_predict_hash(const uint2* __restrict__ tiles, uint32_t ntiles,
@@ -352,7 +373,7 @@ __global__ void k_reorder(const uint2* __restrict__ tiles, uint32_t ntiles,
     // the cell index travelled with the entry: k_predict_hash (or the fused
     // prediction) computed it from this same prediction
     const uint32_t cell = me.x;
-    const uint32_t key = S.base + fastmod(cell, S.fm, S.n);
+    const uint32_t key = table_key(S, cell);
     const uint32_t b0 = start[key], b1 = start[key + 1];
     if (slot < b0 || slot >= b1) {
       flag(status, kStatusRange);
@@ -398,13 +419,13 @@ __device__ __forceinline__ uint2 bucket_run(uint32_t cell, uint32_t b0,
   return make_uint2(first, len);
 }
 
-// For each cell (its first slot), the runs of its 27 neighbour cells as 9
-// rows (dy, dz) of three x-runs. The x-neighbours of a row have consecutive
-// cell indices, hence consecutive keys; when their runs are adjacent in the
-// layout (their buckets hold no other cell -- the usual case inside the box)
-// the row is stored as one run flagged kRunMerged in its first entry (its
-// other two entries are left unwritten: a third of the table's stores, which
-// the readers skip). Lanes take (cell, row)
+// For each cell (its first slot) of a scene with a bucket key table, the
+// runs of its 27 neighbour cells as 9 rows (dy, dz) of three x-runs. The
+// x-neighbours of a row have consecutive cell indices, hence consecutive
+// keys; when their runs are adjacent in the layout (their buckets hold no
+// other cell -- the usual case inside the box) the row is stored as one run
+// flagged kRunMerged in its first entry (its other two entries are left
+// unwritten: a third of the table's stores, which the readers skip). Lanes take (cell, row)
 // pairs of the warp's tile in parallel; the warp's cell leaders are listed
 // in shared memory (kCellTableBlock threads per block).
 constexpr int kCellTableBlock = 256;
@@ -422,6 +443,7 @@ k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
     const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
+    if (S.direct) continue;  // its rows come from the start table
     const uint32_t i = tile.y + lane;
     const bool live = lane < tile_len(tile);
     const bool leader = live && cell_first[i] == i;
@@ -435,12 +457,13 @@ k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
       const uint32_t slot = tile.y + lead[c];
       const uint32_t dy = w / 3u - 1u, dz = w % 3u - 1u;  // mod 2^32
       const uint32_t mid = __ldg(hash_s + slot) + dy * S.gwy + dz * S.gwz;
+      uint2* out = cell_tab + static_cast<uint64_t>(slot) * 27u + 3u * w;
       // keys of mid - 1, mid, mid + 1: neighbours of mid's key modulo n,
       // except across the 2^32 wrap of the index
       const uint32_t km = fastmod(mid, S.fm, S.n);
       const uint32_t kl = mid == 0u ? kmax : (km == 0u ? S.n - 1u : km - 1u);
       const uint32_t kh = mid == 0xffffffffu ? 0u : (km + 1u == S.n ? 0u : km + 1u);
-      const uint32_t* st = start + S.base;
+      const uint32_t* st = start + S.tbase;
       const uint32_t l0 = __ldg(st + kl), l1 = __ldg(st + kl + 1);
       const uint32_t m0 = kl + 1u == km ? l1 : __ldg(st + km);
       const uint32_t m1 = __ldg(st + km + 1);
@@ -465,7 +488,6 @@ k_cell_table(const uint2* __restrict__ tiles, uint32_t ntiles,
           adjacent = false;
         }
       }
-      uint2* out = cell_tab + static_cast<uint64_t>(slot) * 27u + 3u * w;
       if (adjacent) {
         out[0] = make_uint2(f, (e - f) | kRunMerged);
       } else {
@@ -511,11 +533,16 @@ __device__ __forceinline__ void density_store(const SceneDev& S, uint32_t i,
 // Thread-per-particle form in one pass: each lane walks its cell's runs,
 // classifies every candidate (FMA estimate, exact d2 inside the 2e-6 band)
 // and accumulates the density and its list as it goes. Lanes of one cell
-// walk identical runs, so their loads coincide.
-__global__ void k_density_walk(const uint2* __restrict__ tiles,
+// walk identical runs, so their loads coincide. The walk is issue-bound and
+// runs at 32 registers (64 warps per SM); the direct rows' arithmetic would
+// take it to 36 unless capped (with no spills; the mixed form spills a few
+// row values).
+template <int kTables>
+__global__ void __maxnreg__(32) k_density_walk(const uint2* __restrict__ tiles,
                                uint32_t ntiles,
                                const SceneDev* __restrict__ scenes,
                                const float4* __restrict__ pred,
+                               const uint32_t* __restrict__ start,
                                const uint32_t* __restrict__ cell_first,
                                const uint2* __restrict__ cell_tab,
                                float2* __restrict__ dens_a,
@@ -536,7 +563,8 @@ __global__ void k_density_walk(const uint2* __restrict__ tiles,
     uint32_t cnt = 0;
     uint32_t* wp = nbr + i;  // next list entry (a bumped pointer is the
                              // cheapest append in the hit path)
-    walk_runs(cell_tab, cell_first[i], pred, [&](uint32_t j, float4 q) {
+    const uint32_t cf = kTables == kTablesDirect ? 0u : cell_first[i];
+    walk_runs<kTables>(S, start, cell_tab, cf, __float_as_uint(me.w), pred, [&](uint32_t j, float4 q) {
       const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
       const float d2f = dist2_fast(dx, dy, dz);
       if (d2f <= S.cut_hi && j != i) {
@@ -572,6 +600,7 @@ template <int kChunks>
 __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
                           const SceneDev* __restrict__ scenes,
                           const float4* __restrict__ pred,
+                          const uint32_t* __restrict__ start,
                           const uint32_t* __restrict__ cell_first,
                           const uint2* __restrict__ cell_tab,
                           float2* __restrict__ dens_a,
@@ -599,8 +628,14 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
       cells &= cells - 1;
       const int c1 = cells ? __ffs(cells) - 1 : static_cast<int>(live_end);
       const uint32_t cfc = __shfl_sync(kFull, cf, c0);
+      const uint32_t cellc = __shfl_sync(kFull, __float_as_uint(me.w), c0);
       uint2 run = make_uint2(0u, 0u);
-      if (lane < 27) run = __ldg(cell_tab + static_cast<uint64_t>(cfc) * 27u + lane);
+      if (S.direct) {
+        if (lane < 27u && lane % 3u == 0u)
+          run = direct_row(S, start, S.tbase + cellc - S.gwy - S.gwz, static_cast<int>(lane / 3u));
+      } else if (lane < 27) {
+        run = __ldg(cell_tab + static_cast<uint64_t>(cfc) * 27u + lane);
+      }
       // a merged row keeps its run in its first entry; the other two are unused
       const uint32_t heads =
           __ballot_sync(kFull, lane < 27u && lane % 3u == 0u && (run.y & kRunMerged));
@@ -671,7 +706,8 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
       cnt = kept;
     } else {
       // list overflow: sum directly; the force passes walk the runs too
-      walk_runs(cell_tab, cf, pred, [&](uint32_t j, float4 q) {
+      walk_runs<kTablesMixed>(S, start, cell_tab, cf, __float_as_uint(me.w), pred,
+                              [&](uint32_t j, float4 q) {
         const float d2 = dist2(q.x - p.x, q.y - p.y, q.z - p.z);
         if (j != i && d2 <= S.cut_lt) density_pair(S, d2, s2, s3);
       });
@@ -708,10 +744,11 @@ __device__ __forceinline__ void pressure_pair(const SceneDev& S, float3 p,
 
 
 
-template <int kGather>
+template <int kGather, int kTables>
 __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
                            const SceneDev* __restrict__ scenes,
                            const float4* __restrict__ pred,
+                           const uint32_t* __restrict__ start,
                            const uint32_t* __restrict__ cell_first,
                            const uint2* __restrict__ cell_tab,
                            const float2* __restrict__ dens_a,
@@ -755,7 +792,8 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
           if (k0 + u < cnt) pressure_pair(S, p, Pi, Pni, q[u], b[u], f);
       }
     } else {
-      walk_runs(cell_tab, cell_first[i], pred, [&](uint32_t j, float4 q) {
+      walk_runs<kTables>(S, start, cell_tab, cell_first[i], __float_as_uint(pi.w), pred,
+                         [&](uint32_t j, float4 q) {
         if (j == i) return;
         const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
         if (dist2(dx, dy, dz) <= S.cut_le)
@@ -792,10 +830,11 @@ __device__ __forceinline__ void visc_pair(const SceneDev& S, float3 p,
   }
 }
 
-template <int kGather>
+template <int kGather, int kTables>
 __global__ void k_visc_integrate(
     const uint2* __restrict__ tiles, uint32_t ntiles,
     const SceneDev* __restrict__ scenes, const float4* __restrict__ pred,
+    const uint32_t* __restrict__ start,
     const uint32_t* __restrict__ cell_first, const uint2* __restrict__ cell_tab,
     const uint32_t* __restrict__ nbr, const uint32_t* __restrict__ ncount,
     uint32_t nbr_stride, uint32_t nbr_cap, const float4* __restrict__ rec_v,
@@ -835,7 +874,8 @@ __global__ void k_visc_integrate(
             if (k0 + u < cnt) visc_pair(S, p, vi, q[u], vj[u], f);
         }
       } else {
-        walk_runs(cell_tab, cell_first[i], pred, [&](uint32_t j, float4 q) {
+        walk_runs<kTables>(S, start, cell_tab, cell_first[i], __float_as_uint(pi.w), pred,
+                           [&](uint32_t j, float4 q) {
           if (j != i) visc_pair(S, p, vi, q, __ldg(rec_v + 2ull * j + 1), f);
         });
       }
@@ -860,7 +900,8 @@ __global__ void k_visc_integrate(
         if (id < S.n) out4[S.base + id] = make_float4(x.x, x.y, x.z, 0.34f);
         else bad = true;
       }
-      if (fuse_next) predict_key(S, x, v4, key, cell);
+      // the grid constants are read here, not kept in registers through the loop
+      if (fuse_next) predict_key(scenes[tile_scene(tile)], x, v4, key, cell);
     }
     if (fuse_next) {
       const uint32_t r = aggregated_rank(count, key, live);
@@ -1117,9 +1158,9 @@ cudaError_t launch_scan(const LaunchCtx& c, uint32_t len, cudaStream_t st) {
   return e;
 }
 
-int kernels_per_substep(uint32_t keys) {
+int kernels_per_substep(uint32_t keys, int tables) {
   const uint32_t nb = (keys + kScanBlock - 1) / kScanBlock;
-  return nb <= kScanFoldBlocks ? 8 : 9;
+  return (nb <= kScanFoldBlocks ? 8 : 9) - (tables == kTablesDirect ? 1 : 0);
 }
 
 uint32_t scan_partials_needed(uint64_t len) {
@@ -1139,7 +1180,7 @@ cudaError_t launch_sort_reorder(const LaunchCtx& c, const Tiles& old_tiles,
                    c.block_misc, st, new_tiles.d, new_tiles.n, c.scenes, c.tmp_hi,
                    c.tmp_src, c.start, c.pos, c.vel, c.pos2, c.vel2, c.pred,
                    c.hash_s, c.cell_first, c.src_limit, c.status);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && c.tables != kTablesDirect)
       e = launch_pdl(c.pdl, k_cell_table, grid_for(new_tiles.n, kCellTableBlock, c.max_blocks),
                      kCellTableBlock, st, new_tiles.d, new_tiles.n, c.scenes,
                      c.hash_s, c.cell_first, c.start, c.cell_tab);
@@ -1153,26 +1194,45 @@ cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
   const int b = c.block_nbr;
   const uint32_t g = grid_for(tiles.n, b, c.max_blocks);
   if (c.cell_tile <= 1)
-    return launch_pdl(c.pdl, k_density_walk, g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
-                      c.cell_first, c.cell_tab, c.dens_a, c.dens_b, c.nbr,
+    return launch_pdl(c.pdl,
+                      c.tables == kTablesDirect    ? k_density_walk<kTablesDirect>
+                      : c.tables == kTablesBuckets ? k_density_walk<kTablesBuckets>
+                                                   : k_density_walk<kTablesMixed>,
+                      g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
+                      c.start, c.cell_first, c.cell_tab, c.dens_a, c.dens_b, c.nbr,
                       c.ncount, c.nbr_stride, c.nbr_cap);
   auto kern = c.cell_tile <= 64    ? k_density<2>
               : c.cell_tile <= 128 ? k_density<4>
               : c.cell_tile <= 192 ? k_density<6>
                                    : k_density<8>;
   return launch_pdl(c.pdl, kern, g, b, st, tiles.d, tiles.n, c.scenes, c.pred,
-                    c.cell_first, c.cell_tab, c.dens_a, c.dens_b, c.nbr,
+                    c.start, c.cell_first, c.cell_tab, c.dens_a, c.dens_b, c.nbr,
                     c.ncount, c.nbr_stride, c.nbr_cap);
+}
+
+// The instantiation for the launch's gather batch (2, 4, 8) and table forms,
+// from nine listed as (direct, buckets, mixed) x (2, 4, 8).
+template <class K>
+K pick_gather_tables(const LaunchCtx& c, K d2, K d4, K d8, K b2, K b4, K b8, K m2, K m4,
+                     K m8) {
+  const int g = c.gather == 2 ? 0 : c.gather == 8 ? 2 : 1;
+  const K direct[3] = {d2, d4, d8}, buckets[3] = {b2, b4, b8}, mixed[3] = {m2, m4, m8};
+  return c.tables == kTablesDirect    ? direct[g]
+         : c.tables == kTablesBuckets ? buckets[g]
+                                      : mixed[g];
 }
 
 cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
                             cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_force;
-  auto kern = c.gather == 2 ? k_pressure<2> : c.gather == 8 ? k_pressure<8>
-                                                           : k_pressure<4>;
+  auto kern = pick_gather_tables<decltype(&k_pressure<4, kTablesMixed>)>(
+      c, k_pressure<2, kTablesDirect>, k_pressure<4, kTablesDirect>, k_pressure<8, kTablesDirect>,
+      k_pressure<2, kTablesBuckets>, k_pressure<4, kTablesBuckets>,
+      k_pressure<8, kTablesBuckets>, k_pressure<2, kTablesMixed>, k_pressure<4, kTablesMixed>,
+      k_pressure<8, kTablesMixed>);
   return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
-                    tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab,
+                    tiles.n, c.scenes, c.pred, c.start, c.cell_first, c.cell_tab,
                     c.dens_a, c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap,
                     c.vel2, c.rec_v, c.dbg_accp);
 }
@@ -1182,11 +1242,14 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                                   cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_force;
-  auto kern = c.gather == 2   ? k_visc_integrate<2>
-              : c.gather == 8 ? k_visc_integrate<8>
-                              : k_visc_integrate<4>;
+  auto kern = pick_gather_tables<decltype(&k_visc_integrate<4, kTablesMixed>)>(
+      c, k_visc_integrate<2, kTablesDirect>, k_visc_integrate<4, kTablesDirect>,
+      k_visc_integrate<8, kTablesDirect>, k_visc_integrate<2, kTablesBuckets>,
+      k_visc_integrate<4, kTablesBuckets>, k_visc_integrate<8, kTablesBuckets>,
+      k_visc_integrate<2, kTablesMixed>, k_visc_integrate<4, kTablesMixed>,
+      k_visc_integrate<8, kTablesMixed>);
   return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
-                    tiles.n, c.scenes, c.pred, c.cell_first, c.cell_tab, c.nbr,
+                    tiles.n, c.scenes, c.pred, c.start, c.cell_first, c.cell_tab, c.nbr,
                     c.ncount, c.nbr_stride, c.nbr_cap, c.rec_v, c.pos2, c.vel2,
                     write_out ? c.out4 : nullptr, fuse_next, c.count, c.keyrank,
                     c.dbg_velv, c.status);

@@ -37,6 +37,10 @@ struct Tiles {
 };
 
 // Device buffers and launch shape used by one engine.
+// Key-table forms present in a launch: the neighbour kernels are compiled
+// for direct tables only, bucket tables only, or both (chosen per scene).
+enum TableForms : int { kTablesMixed = 0, kTablesDirect = 1, kTablesBuckets = 2 };
+
 struct LaunchCtx {
   const SceneDev* scenes = nullptr;
   float4* pos = nullptr;   // state A (read at substep start)
@@ -63,6 +67,7 @@ struct LaunchCtx {
   int gather = 4;               // neighbour entries gathered per batch (2, 4, 8)
   int cell_tile = 1;            // density-pass candidates held per cell tile
                                 // (1: thread-per-particle walk)
+  int tables = kTablesMixed;    // key-table forms of the live scenes
   float4* out4 = nullptr;
   uint32_t* status = nullptr;
   float4* dbg_accp = nullptr;   // captured substep: per-slot intermediates
@@ -109,9 +114,10 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                                   cudaStream_t st);
 
 // Kernels launched by one substep over a key table of `keys` entries (scan 2
-// or 3, scatter, reorder, cell table, density, pressure, viscosity), and by
-// the standalone prediction of a step's first substep.
-int kernels_per_substep(uint32_t keys);
+// or 3, scatter, reorder, cell table unless every table is direct, density,
+// pressure, viscosity), and by the standalone prediction of a step's first
+// substep.
+int kernels_per_substep(uint32_t keys, int tables);
 constexpr int kKernelsPredict = 1;
 cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
                           const float4* vel, const float2* dens, float* opos,

@@ -61,7 +61,7 @@ class Tuning(ctypes.Structure):
     """struct sph_tuning."""
     _fields_ = [("block", ctypes.c_int32), ("cell_tile", ctypes.c_int32),
                 ("particles_per_warp", ctypes.c_int32), ("gather", ctypes.c_int32),
-                ("force_block", ctypes.c_int32)]
+                ("force_block", ctypes.c_int32), ("table", ctypes.c_int32)]
 
 
 class View(ctypes.Structure):

@@ -226,8 +226,8 @@ class FluidSimulation:
         return int(self._lib.sph_kernel_launches(self._h))
 
     def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4,
-                   force_block=0):
-        t = Tuning(block, cell_tile, particles_per_warp, gather, force_block)
+                   force_block=0, table=0):
+        t = Tuning(block, cell_tile, particles_per_warp, gather, force_block, table)
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), self._h)
 
     def tuning(self):
@@ -235,7 +235,7 @@ class FluidSimulation:
         check(self._lib.sph_get_tuning(self._h, ctypes.byref(t)), self._h)
         return dict(block=t.block, cell_tile=t.cell_tile,
                     particles_per_warp=t.particles_per_warp, gather=t.gather,
-                    force_block=t.force_block)
+                    force_block=t.force_block, table=t.table)
 
     def autotune(self, deltatime, substeps=1, steps_per_trial=2):
         """Sweep the launch configuration on real steps and keep the fastest;
@@ -249,7 +249,7 @@ class FluidSimulation:
         self._cache = None
         return dict(block=t.block, cell_tile=t.cell_tile,
                     particles_per_warp=t.particles_per_warp, gather=t.gather,
-                    force_block=t.force_block), float(ms.value)
+                    force_block=t.force_block, table=t.table), float(ms.value)
 
     @property
     def handle(self):
@@ -458,8 +458,8 @@ class Batch:
         return rgba, depth
 
     def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4,
-                   force_block=0):
-        t = Tuning(block, cell_tile, particles_per_warp, gather, force_block)
+                   force_block=0, table=0):
+        t = Tuning(block, cell_tile, particles_per_warp, gather, force_block, table)
         self._check(self._lib.sph_batch_set_tuning(self._h, ctypes.byref(t)))
 
     def tuning(self):
@@ -467,7 +467,7 @@ class Batch:
         self._check(self._lib.sph_batch_get_tuning(self._h, ctypes.byref(t)))
         return dict(block=t.block, cell_tile=t.cell_tile,
                     particles_per_warp=t.particles_per_warp, gather=t.gather,
-                    force_block=t.force_block)
+                    force_block=t.force_block, table=t.table)
 
     def autotune(self, substeps: int, steps_per_trial: int = 2):
         """Sweep the launch configuration on real steps of the resident
@@ -480,7 +480,7 @@ class Batch:
                                                  self._stream))
         return dict(block=t.block, cell_tile=t.cell_tile,
                     particles_per_warp=t.particles_per_warp, gather=t.gather,
-                    force_block=t.force_block), float(ms.value)
+                    force_block=t.force_block, table=t.table), float(ms.value)
 
     def profile_enable(self, on=True):
         self._check(self._lib.sph_batch_profile_enable(self._h, 1 if on else 0))

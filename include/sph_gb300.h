@@ -74,6 +74,16 @@ typedef struct sph_tuning {
                          kernels issue together: 2, 4 or 8 (default 4)    */
   int32_t force_block; /* threads per block of the pressure and viscosity
                           kernels (multiple of 32, 32..1024); 0 = block   */
+  int32_t table;      /* key table of the sort: 0 = one entry per cell of
+                         the scene's grid where the grid has at most two
+                         cells per particle, else n entries (cell index
+                         mod n); 1 = n entries for every scene; 2 = as 0,
+                         and grid tables for larger grids too while an
+                         allowance of 65,536 extra entries lasts (scenes
+                         in layout order). Results agree to rounding; they
+                         are bit-identical unless a predicted position lies
+                         more than one cell beyond the box (or the box
+                         spans more than 32,764 cells along an axis)      */
 } sph_tuning;
 
 /* Reference defaults of physicsWorld.h:96-106,145 and physicsWorld.cc:47,87. */

@@ -28,15 +28,19 @@ def run_substep(fx, params, debug=True, tuning=None):
     return got, pos, vel, dens
 
 
+@pytest.mark.parametrize("table", [0, 1, 2])
 @pytest.mark.parametrize("name", substep_fixtures())
-def test_substep_parity(gpu_lib, name):
+def test_substep_parity(gpu_lib, name, table):
+    """Every fixture under each key-table form: automatic, n buckets
+    (cell index mod n), and one entry per grid cell wherever the table
+    buffers have room (the small fixtures' 16^3 grids included)."""
     fx = load_fixture(name)
     p = fixture_params(fx)
     fx["bound"] = np.array(p.bound, np.float64)
-    got, pos, vel, dens = run_substep(fx, p)
+    got, pos, vel, dens = run_substep(fx, p, tuning=dict(table=table))
     assert np.array_equal(got["dens"], dens)
     rep = compare_substep(got, fx, float(fx["dt"]), pos, vel)
-    print(name, rep)
+    print(name, table, rep)
 
 
 @pytest.mark.parametrize("tile", [64, 128, 192, 256])
@@ -56,14 +60,16 @@ def test_substep_parity_cooperative_density(gpu_lib, name, tile):
     print(name, tile, rep)
 
 
-def test_large_scene_parity(gpu_lib):
+@pytest.mark.parametrize("table", [0, 1])
+def test_large_scene_parity(gpu_lib, table):
     """1M-particle dam break: full keys / hashes / start table / sorted order
-    bit-exact (digests), sampled particles within tolerance."""
+    bit-exact (digests), sampled particles within tolerance; with its grid
+    table (automatic) and with n buckets."""
     from fluidsim import scenes
     fx = load_fixture("substep_dam_break_1m_sample.npz")
     sc = scenes.dam_break_1m()
     full = dict(pos_in=sc["pos"], vel_in=sc["vel"], dt=fx["dt"])
-    got, pos, vel, dens = run_substep(full, sc["params"])
+    got, pos, vel, dens = run_substep(full, sc["params"], tuning=dict(table=table))
     sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
     assert sha(got["hash"]) == str(fx["hash_digest"])
     assert sha(got["key"]) == str(fx["key_digest"])
@@ -92,6 +98,39 @@ def test_deterministic(gpu_lib):
         sim.close()
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
+
+
+def test_table_forms_agree(gpu_lib):
+    """The 16k dam break (a grid table by default) stepped with each key
+    table form: the walks visit the same particles in the same order, so the
+    states are bit-identical."""
+    import fluidsim
+    from fluidsim import scenes
+    sc = scenes.dam_break_16k()
+    outs = []
+    for table in (0, 1, 2):
+        sim = fluidsim.FluidSimulation(sc["params"])
+        sim.InitializeData(sc["pos"].shape[0], sc["pos"], sc["vel"])
+        sim.set_tuning(table=table)
+        assert sim.tuning()["table"] == table
+        for _ in range(6):
+            sim.Update(sc["dt"], sc["substeps"])
+        assert sim.status() == 0
+        outs.append(sim.download())
+        sim.close()
+    # switching forms between steps (new keys, a new table length, the
+    # captured graphs and the carried prediction dropped) changes nothing
+    sim = fluidsim.FluidSimulation(sc["params"])
+    sim.InitializeData(sc["pos"].shape[0], sc["pos"], sc["vel"])
+    for k in range(6):
+        sim.set_tuning(table=(0, 1, 2)[k % 3])
+        sim.Update(sc["dt"], sc["substeps"])
+    assert sim.status() == 0
+    outs.append(sim.download())
+    sim.close()
+    for other in outs[1:]:
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
 
 
 def test_out_positions_buffer(gpu_lib):
