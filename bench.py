@@ -45,8 +45,9 @@ UNIT = "particle-steps/s"
 # writes of its inputs and outputs once), for the roofline.
 ALG_BYTES = {
     "predict_hash": 44,   # pos 16 + vel 16 in; key/rank 8 + count 4 out
-    "spatial": 172,       # scan 12 + scatter 24 + reorder 96 + cell table ~40
-                          # (216 B of row runs per cell, ~5.4 particles a cell)
+    "spatial": 172,       # scan 12 per key-table entry + scatter 24 + reorder 96
+                          # + cell table ~40 (216 B of row runs per cell, ~5.4
+                          # particles a cell); spatial_bytes() gives the scene's
     "density": 44,        # pred 16 + start 4 in; dens_a 8 + dens_b 16 out
     "pressure": 76,       # pred 16, start 4, dens_a 8, dens_b 16, vel 16 in; velp 16 out
     "viscosity": 84,      # pred 16, start 4, velp 16, pos 16 in; pos 16 + vel 16 out
@@ -54,6 +55,13 @@ ALG_BYTES = {
     # half is a copy, so it is not counted as compulsory)
 }
 SURVEY_BYTES_PER_SUBSTEP = 300  # idealised whole-substep traffic per particle
+
+
+def spatial_bytes(grid: bool, entries: int, n: int) -> float:
+    """Algorithmic bytes per particle of the sort phase for a key table of
+    `entries` entries: a grid table (one entry per cell) needs no cell-table
+    kernel, a bucket table (n entries) does."""
+    return 12.0 * entries / n + 24 + 96 + (0 if grid else 40)
 PHASES = ["predict_hash", "spatial", "density", "pressure", "viscosity"]
 
 
@@ -453,18 +461,20 @@ def run_native(args):
     share = {nm: phase[i] / max(phase[:5].sum(), 1e-12) for i, nm in enumerate(names)}
     dom = max(["density", "pressure", "viscosity"], key=lambda k: per_launch_ms[k])
     peak, peak_kind = peaks()
-    achieved = ALG_BYTES[dom] * n / (per_launch_ms[dom] / 1000.0) / 1e9
+    grid, entries = fluidsim.simulation.key_table(sc["params"], n, sim_tuning["table"])
+    alg = dict(ALG_BYTES, spatial=spatial_bytes(grid, entries, n))
+    achieved = alg[dom] * n / (per_launch_ms[dom] / 1000.0) / 1e9
     tr = ncu_traffic(args.workload, dom)
     # every phase against the same peak: the sort (scan, scatter, reorder,
     # cell table), density and the two force kernels; the prediction is
     # fused into the viscosity kernel while it is carried between steps
     phase_roofline = {}
     for nm in ["spatial", "density", "pressure", "viscosity"]:
-        ach = ALG_BYTES[nm] * n / (per_launch_ms[nm] / 1000.0) / 1e9
-        parts = {"spatial": ["reorder", "cell_table"]}.get(nm, [nm])
+        ach = alg[nm] * n / (per_launch_ms[nm] / 1000.0) / 1e9
+        parts = {"spatial": ["reorder"] + ([] if grid else ["cell_table"])}.get(nm, [nm])
         tp = [ncu_traffic(args.workload, k) for k in parts]
         phase_roofline[nm] = {
-            "ms_per_launch": per_launch_ms[nm], "alg_bytes_per_particle": ALG_BYTES[nm],
+            "ms_per_launch": per_launch_ms[nm], "alg_bytes_per_particle": alg[nm],
             "achieved_GBps": ach, "frac": ach / peak,
             "dram_bytes_per_particle": (sum(tp) if all(x is not None for x in tp) else None),
             "dram_bytes_of": "+".join(parts)}
@@ -478,12 +488,13 @@ def run_native(args):
         "config": {"workload": args.workload, "particles": n, "substeps": S,
                    "dt": dt, "parallelism": f"replicas{world}" if world > 1 else "single",
                    "l2": "flushed (256 MiB write) before every timed step",
-                   "tuning": tuning or sim_tuning},
+                   "tuning": tuning or sim_tuning,
+                   "key_table": {"form": "grid" if grid else "buckets", "entries": entries}},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
-                     "alg_bytes_per_particle": ALG_BYTES[dom],
+                     "alg_bytes_per_particle": alg[dom],
                      "traffic": (tr * n if tr is not None else None),
                      "timing": "CUDA events around each kernel phase on the "
                                "library's stream, over a second pass of the "

@@ -168,11 +168,24 @@ __device__ __forceinline__ void walk_runs(const SceneDev& S,
   const bool direct = kTables == kTablesDirect    ? true
                     : kTables == kTablesBuckets ? false
                                                 : S.direct != 0u;
-  const uint2* row = cell_tab + static_cast<uint64_t>(direct ? 0u : cf) * 27u;
-  const uint32_t k0 = S.tbase + cell - S.gwy - S.gwz;
+  if (direct) {
+    // rows (dy, dz) in the cell table's order (dz fastest); k = the row's
+    // middle cell
+    uint32_t k = S.tbase + cell - S.gwy - S.gwz;
+    int dz = 0;
+#pragma unroll 1
+    for (int w = 0; w < 9; ++w) {
+      const uint32_t e = __ldg(start + k + 2);
+#pragma unroll 1
+      for (uint32_t j = __ldg(start + k - 1); j < e; ++j) visit(j, __ldg(pred + j));
+      if (++dz == 3) { dz = 0; k += S.gwy - 2u * S.gwz; } else { k += S.gwz; }
+    }
+    return;
+  }
+  const uint2* row = cell_tab + static_cast<uint64_t>(cf) * 27u;
 #pragma unroll 1
   for (int w = 0; w < 9; ++w, row += 3) {
-    const uint2 m = direct ? direct_row(S, start, k0, w) : __ldg(row);
+    const uint2 m = __ldg(row);
     if (m.y & kRunMerged) {
       const uint32_t e = m.x + (m.y & ~kRunMerged);
 #pragma unroll 1
@@ -1119,8 +1132,8 @@ k_import_rows(uint32_t first, uint32_t n, const float* __restrict__ ipos,
 // ------------------------------------------------------------- launchers
 // Substep kernels go out with programmatic stream serialisation: the next
 // kernel is scheduled during its predecessor's last wave and waits for it in
-// pdl_enter(), which hides the launch and ramp-up between the nine kernels
-// of a substep (inside a graph these become programmatic edges).
+// pdl_enter(), which hides the launch and ramp-up between the seven to nine
+// kernels of a substep (inside a graph these become programmatic edges).
 template <class... KArgs, class... Args>
 cudaError_t launch_pdl(bool pdl, void (*kernel)(KArgs...), uint32_t grid, int block,
                        cudaStream_t st, Args... args) {

@@ -65,6 +65,34 @@ def _stream(stream):
     return ctypes.c_void_p(int(getattr(stream, "cuda_stream", stream)))
 
 
+def key_table(params, n: int, table: int = 0):
+    """(grid, entries) of the key table the engine gives a scene of n
+    particles stepped alone under tuning.table = `table`: one entry per cell
+    of its internal grid (grid = True) when the grid has at most two cells per
+    particle -- or, with table 2, when its excess over n fits the 65,536-entry
+    allowance -- else n bucket entries. Mirrors the engine's GridAxis and
+    UploadScenes (csrc/sph_engine.cu)."""
+    p = to_params(params)
+    r = float(np.float32(p.radius))
+
+    def axis(b):
+        h = float(np.float32(b) * np.float32(0.5))
+        a, c = -h / r, h / r
+        if not (math.isfinite(a) and math.isfinite(c)):
+            return 1024
+        lo, hi = min(math.floor(a), math.floor(c)) - 2, max(math.floor(a), math.floor(c)) + 2
+        if lo < -1e9 or hi > 1e9:
+            return 1024
+        return int(min(hi - lo + 1, 32768))
+
+    cells = axis(p.bound[0]) * axis(p.bound[1]) * axis(p.bound[2])
+    if table != 1 and cells <= 2 * n:
+        return True, cells
+    if table == 2 and cells - n <= 65536:
+        return True, cells
+    return False, n
+
+
 def grid_arrangement(n: int, gap: float = 0.215):
     """Default lattice of InitializeData / GridArrangement
     (physicsWorld.cc:139-142, 518-557), in float32 like the reference."""

@@ -133,6 +133,36 @@ def test_table_forms_agree(gpu_lib):
             assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("scene,table", [("dam_break_16k", 0), ("dam_break_16k", 1),
+                                         ("substep_cell_boundaries.npz", 0),
+                                         ("substep_cell_boundaries.npz", 2)])
+def test_key_table_choice(gpu_lib, scene, table):
+    """fluidsim.simulation.key_table predicts the engine's table form: a
+    substep over a grid table launches no cell-table kernel, so it runs one
+    kernel fewer (a carried prediction: no prediction kernel either)."""
+    import fluidsim
+    from fluidsim import scenes
+    from fluidsim.simulation import key_table
+    if scene.endswith(".npz"):
+        fx = load_fixture(scene)
+        params, pos, vel = fixture_params(fx), fx["pos_in"], fx["vel_in"]
+    else:
+        sc = getattr(scenes, scene)()
+        params, pos, vel = sc["params"], sc["pos"], sc["vel"]
+    n = pos.shape[0]
+    grid, entries = key_table(params, n, table)
+    sim = fluidsim.FluidSimulation(params)
+    sim.InitializeData(n, pos, vel)
+    sim.set_tuning(table=table)
+    sim.Update(1 / 120, 1)
+    k0 = sim.kernel_launches()
+    sim.Update(1 / 120, 1)
+    scan = 2 if (entries + 2047) // 2048 <= 4096 else 3
+    assert sim.kernel_launches() - k0 == scan + 6 - (1 if grid else 0)
+    assert sim.status() == 0
+    sim.close()
+
+
 def test_out_positions_buffer(gpu_lib):
     """OutPositions (physicsWorld.cc:107): float4 (pos, 0.34) in caller order."""
     import ctypes
