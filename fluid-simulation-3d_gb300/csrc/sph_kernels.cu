@@ -263,17 +263,27 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x,
   return before + incl - x;
 }
 
+// The kScanItems (= 4) consecutive counts of a thread: one 16-byte load
+// inside the table, element loads at its ragged end.
+__device__ __forceinline__ uint4 load_counts(const uint32_t* __restrict__ count, uint32_t b0,
+                                             uint32_t len) {
+  if (b0 + 4u <= len) return *reinterpret_cast<const uint4*>(count + b0);
+  uint4 v = make_uint4(0u, 0u, 0u, 0u);
+  if (b0 < len) v.x = count[b0];
+  if (b0 + 1u < len) v.y = count[b0 + 1u];
+  if (b0 + 2u < len) v.z = count[b0 + 2u];
+  return v;
+}
+
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_reduce(const uint32_t* __restrict__ count, uint32_t len,
               uint32_t* __restrict__ partial) {
+  static_assert(kScanItems == 4, "one uint4 of counts per thread");
   pdl_enter();
   const uint32_t b0 = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
-  uint32_t s = 0;
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k)
-    if (b0 + k < len) s += count[b0 + k];
+  const uint4 v = load_counts(count, b0, len);
   uint32_t total;
-  block_excl_scan(s, &total);
+  block_excl_scan(v.x + v.y + v.z + v.w, &total);
   if (threadIdx.x == 0) partial[blockIdx.x] = total;
 }
 
@@ -296,39 +306,60 @@ k_scan_partials(uint32_t* __restrict__ partial, uint32_t nb,
 // Down-sweep. With `fold` the block totals in `partial` are raw (no
 // k_scan_partials): each block sums the totals before it itself -- O(nb^2)
 // reads in all, so the launcher folds only up to kScanFoldBlocks blocks --
-// and the last block writes the grand total start[len].
+// and the last block writes the grand total start[len]. The block's own
+// counts are loaded first, so their latency overlaps the fold's reads, and
+// one block pass both scans the counts and sums the fold.
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_down(uint32_t* __restrict__ count, uint32_t len,
             const uint32_t* __restrict__ partial, uint32_t nb, int fold,
             uint32_t* __restrict__ start) {
+  __shared__ uint32_t warp_scan[kScanThreads / 32], warp_fold[kScanThreads / 32];
   pdl_enter();
-  uint32_t base;
-  if (fold) {
-    uint32_t s = 0;
-    for (uint32_t c = threadIdx.x; c < blockIdx.x; c += kScanThreads) s += partial[c];
-    block_excl_scan(s, &base);
-  } else {
-    base = partial[blockIdx.x];
-  }
   const uint32_t b0 = blockIdx.x * kScanBlock + threadIdx.x * kScanItems;
-  uint32_t v[kScanItems];
-  uint32_t s = 0;
-#pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    v[k] = (b0 + k < len) ? count[b0 + k] : 0u;
-    s += v[k];
+  const uint4 v = load_counts(count, b0, len);
+  uint32_t f = 0;
+  if (fold) {
+    for (uint32_t c = threadIdx.x; c < blockIdx.x; c += kScanThreads) f += partial[c];
   }
-  uint32_t total;
-  uint32_t run = block_excl_scan(s, &total) + base;
+  const uint32_t s = v.x + v.y + v.z + v.w;
+  const uint32_t lane = lane_id(), w = threadIdx.x >> 5;
+  const uint32_t incl = warp_incl_scan(s);
 #pragma unroll
-  for (int k = 0; k < kScanItems; ++k) {
-    if (b0 + k < len) {
-      start[b0 + k] = run;
-      count[b0 + k] = 0u;  // ready for the next substep's histogram
+  for (int d = 16; d >= 1; d >>= 1) f += __shfl_xor_sync(kFull, f, d);
+  if (lane == 31) warp_scan[w] = incl;
+  if (lane == 0) warp_fold[w] = f;
+  __syncthreads();
+  constexpr uint32_t kWarps = kScanThreads / 32;
+  uint32_t before = 0, block_total = 0, base = 0;
+#pragma unroll
+  for (uint32_t u = 0; u < kWarps; ++u) {  // smem broadcasts: every lane reads the same word
+    const uint32_t ws = warp_scan[u];
+    before += u < w ? ws : 0u;
+    block_total += ws;
+    base += warp_fold[u];
+  }
+  if (!fold) base = partial[blockIdx.x];
+  uint32_t run = base + before + incl - s;
+  if (b0 + 4u <= len) {
+    uint4 o;
+    o.x = run;
+    o.y = o.x + v.x;
+    o.z = o.y + v.y;
+    o.w = o.z + v.z;
+    *reinterpret_cast<uint4*>(start + b0) = o;
+    *reinterpret_cast<uint4*>(count + b0) = make_uint4(0u, 0u, 0u, 0u);  // next histogram
+  } else {
+    const uint32_t vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+      if (b0 + k < len) {
+        start[b0 + k] = run;
+        count[b0 + k] = 0u;
+      }
+      run += vv[k];
     }
-    run += v[k];
   }
-  if (fold && blockIdx.x + 1 == nb && threadIdx.x == 0) start[len] = base + total;
+  if (fold && blockIdx.x + 1 == nb && threadIdx.x == 0) start[len] = base + block_total;
 }
 
 // ----------------------------------------------------------------- scatter
