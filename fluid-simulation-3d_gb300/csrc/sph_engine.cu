@@ -65,13 +65,13 @@ uint32_t GridAxis(float h, float r, uint32_t* origin) {
 }
 
 // The key table of a scene: one entry per grid cell (a direct table, where a
-// cell's run needs no bucket search) when the grid has at most two cells per
+// cell's run needs no bucket search) when the grid has at most four cells per
 // particle, else n entries holding cell index mod n. The choice depends on
 // the scene alone, so a scene steps bit for bit alike in any batch. The
 // table buffers hold kTablePerParticle entries per particle of capacity plus
 // an allowance that tuning.table = 2 spends on direct tables for scenes with
 // larger grids.
-constexpr uint64_t kDirectCellsPerParticle = 2;
+constexpr uint64_t kDirectCellsPerParticle = 4;
 constexpr uint64_t kTablePerParticle = kDirectCellsPerParticle;
 constexpr uint64_t kTableAllowance = 65536;
 
@@ -172,12 +172,12 @@ int Engine::CudaFail(cudaError_t e, const char* what) {
   } while (0)
 
 int Engine::Init() {
-  // (the key table, 2 entries a particle plus the allowance, is indexed by
-  // 32-bit keys)
-  if (capacity_ == 0 || capacity_ >= (1ull << 31) - kTableAllowance || max_scenes_ == 0 ||
-      max_scenes_ >= (1u << kTileSceneBits))
+  // (the key table, kTablePerParticle entries a particle plus the allowance,
+  // is indexed by 32-bit keys)
+  if (capacity_ == 0 || capacity_ > (0xffffffffull - kTableAllowance) / kTablePerParticle ||
+      max_scenes_ == 0 || max_scenes_ >= (1u << kTileSceneBits))
     return Fail(SPH_ERR_INVALID,
-                "capacity must be in [1, 2^31 - 2^16) and scenes in [1, 2^27)");
+                "capacity must be in [1, 2^30 - 2^14) and scenes in [1, 2^27)");
   int dev = 0;
   SPH_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
   SPH_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, dev),

@@ -68,7 +68,7 @@ def _stream(stream):
 def key_table(params, n: int, table: int = 0):
     """(grid, entries) of the key table the engine gives a scene of n
     particles stepped alone under tuning.table = `table`: one entry per cell
-    of its internal grid (grid = True) when the grid has at most two cells per
+    of its internal grid (grid = True) when the grid has at most four cells per
     particle -- or, with table 2, when its excess over n fits the 65,536-entry
     allowance -- else n bucket entries. Mirrors the engine's GridAxis and
     UploadScenes (csrc/sph_engine.cu)."""
@@ -86,7 +86,7 @@ def key_table(params, n: int, table: int = 0):
         return int(min(hi - lo + 1, 32768))
 
     cells = axis(p.bound[0]) * axis(p.bound[1]) * axis(p.bound[2])
-    if table != 1 and cells <= 2 * n:
+    if table != 1 and cells <= 4 * n:
         return True, cells
     if table == 2 and cells - n <= 65536:
         return True, cells

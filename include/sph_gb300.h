@@ -75,7 +75,7 @@ typedef struct sph_tuning {
   int32_t force_block; /* threads per block of the pressure and viscosity
                           kernels (multiple of 32, 32..1024); 0 = block   */
   int32_t table;      /* key table of the sort: 0 = one entry per cell of
-                         the scene's grid where the grid has at most two
+                         the scene's grid where the grid has at most four
                          cells per particle, else n entries (cell index
                          mod n); 1 = n entries for every scene; 2 = as 0,
                          and grid tables for larger grids too while an
