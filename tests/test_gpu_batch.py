@@ -40,6 +40,34 @@ def test_batch_equals_alone(gpu_lib):
     b.close()
 
 
+def test_mixed_key_tables_batch_equals_alone(gpu_lib):
+    """Scenes with grid key tables next to one with a bucket table (its box
+    three times wider along each axis, so its grid has far more cells than
+    particles): the batch runs the kernels that choose the table per scene,
+    each scene alone the single-form ones, and the results agree bit for
+    bit."""
+    import dataclasses
+    import fluidsim
+    from fluidsim.simulation import key_table
+    scs = small_scenes(4, seed=11)
+    wide = dict(scs[0])
+    wide["params"] = dataclasses.replace(
+        scs[0]["params"], bound=tuple(3.0 * b for b in scs[0]["params"].bound))
+    scs = [wide] + scs[1:]
+    forms = [key_table(s["params"], s["pos"].shape[0])[0] for s in scs]
+    assert forms[0] is False and all(forms[1:])
+    b = fluidsim.Batch(sum(s["pos"].shape[0] for s in scs), 8)
+    ids = [b.add(s["params"], s["pos"], s["vel"], s["dt"]) for s in scs]
+    for _ in range(4):
+        b.step(3)
+    for sid, sc in zip(ids, scs):
+        got = b.download(sid)
+        ref = alone(sc, 4)
+        for g, r in zip(got, ref):
+            assert np.array_equal(g, r)
+    b.close()
+
+
 def test_scenes_join_and_leave_between_steps(gpu_lib):
     import fluidsim
     scs = small_scenes(5, seed=9)
