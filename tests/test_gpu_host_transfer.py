@@ -144,3 +144,43 @@ def test_pinned_upload_prediction_follows_dt_and_substeps(gpu_lib):
         pin.free()
     want = run(lambda shape: np.empty(shape, np.float32))
     assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_upload_into_last_layout_changes_nothing(gpu_lib, pinned):
+    """An upload between steps replaces the whole state: a simulation that
+    has stepped and is then given another state (moved particles, pageable
+    or pinned rows) continues exactly as a fresh simulation given that
+    state -- the carried prediction, the layout and the sort's canonical
+    (cell, caller index) order leave no trace of the earlier steps."""
+    import fluidsim
+    from fluidsim import scenes
+    sc = scenes.dam_break_16k()
+    n = sc["pos"].shape[0]
+    pin = Pinned()
+    host = (lambda a: (lambda b: (b.__setitem__(slice(None), a), b)[1])(pin.array(a.shape))
+            if pinned else a.copy())
+
+    sim = fluidsim.FluidSimulation(sc["params"])
+    sim.InitializeData(n, sc["pos"], sc["vel"])
+    for _ in range(3):
+        sim.Update(sc["dt"], 3)
+    p3, v3, _ = sim.download()
+    rng = np.random.default_rng(4)
+    p3m = (p3 + rng.normal(0, 0.01, p3.shape)).astype(np.float32)  # another state
+    sim.upload(host(p3m), host(v3))
+    for _ in range(2):
+        sim.Update(sc["dt"], 3)
+    a = sim.download()
+    assert sim.status() == 0
+    sim.close()
+
+    fresh = fluidsim.FluidSimulation(sc["params"])
+    fresh.InitializeData(n, p3m, v3)
+    for _ in range(2):
+        fresh.Update(sc["dt"], 3)
+    b = fresh.download()
+    fresh.close()
+    pin.free()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
