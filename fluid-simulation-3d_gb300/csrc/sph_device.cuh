@@ -12,16 +12,22 @@
 //                       cell index, particle index)
 //   tmp_hi[P], tmp_src[P] bucketed (cell index, particle index) and source
 //                       slot, before the order inside each bucket is fixed
-//   count[P], start[P+1] uint32 counting-sort table; a scene owns keys
-//                       [base, base+n) so start[] is also its slot range
-//   cell_tab[27P]       per cell (at its first slot) its neighbour runs as 9
-//                       rows (dy, dz) of 3 runs (dx = -1, 0, +1)
+//   count[4P+2^16], start[4P+2^16+1] uint32 counting-sort key tables; the
+//                       scenes' tables follow one another in layout order
+//                       (scene s owns [tbase, tbase + its table size)), so the
+//                       prefix at a scene's first key is its first slot. A
+//                       table is the scene's grid (one key per cell) or n
+//                       buckets (cell index mod n)
+//   cell_tab[27P]       bucket tables only: per cell (at its first slot) its
+//                       neighbour runs as 9 rows (dy, dz) of 3 runs
+//                       (dx = -1, 0, +1); a grid table's rows are read from
+//                       start[] directly
 //
 // The layout is sorted by an internal cell index, not by the reference's
 // HashCell key: the index is linear in the cell coordinates with x fastest
 // over a grid anchored at the box, so the three x-neighbour cells of a row
-// are consecutive keys and, when their buckets hold only those cells, one
-// contiguous run of slots. Consecutive slots are then spatial neighbours,
+// are consecutive keys and, with a grid table or when their buckets hold only
+// those cells, one contiguous run of slots. Consecutive slots are then spatial neighbours,
 // which the neighbour walks and the force gathers turn into cache hits. The
 // set of pairs within the cutoff does not depend on the key function (every
 // such pair lies in adjacent cells, and a run holds only its own cell), so
