@@ -12,7 +12,7 @@ from parity import compare_substep
 pytestmark = pytest.mark.gpu
 
 
-def random_scene(seed):
+def random_scene(seed, speed=None):
     from fluidsim import scenes
     rng = np.random.default_rng(seed)
     n = int(rng.choice([1, 2, 3, 31, 32, 33, 500, int(rng.integers(100, 3000))]))
@@ -24,7 +24,7 @@ def random_scene(seed):
         pos = centres[rng.integers(0, len(centres), n)] + rng.normal(0, radius, (n, 3))
     else:                     # uniform, 10% of the box width outside it
         pos = rng.uniform(-1.1 * half, 1.1 * half, (n, 3))
-    vel = rng.normal(0, rng.uniform(0.0, 3.0), (n, 3))
+    vel = rng.normal(0, rng.uniform(0.0, 3.0) if speed is None else speed, (n, 3))
     p = scenes.SimParams(radius=radius, bound=bound, **scenes.DAM_CONSTANTS)
     if rng.uniform() < 0.3:
         import dataclasses
@@ -33,12 +33,29 @@ def random_scene(seed):
     return p, pos.astype(np.float32), vel.astype(np.float32), dt
 
 
+@pytest.mark.parametrize("table", [0, 2])
 @pytest.mark.parametrize("seed", range(24))
-def test_random_scene_substep(gpu_lib, oracle_mod, seed):
+def test_random_scene_substep(gpu_lib, oracle_mod, seed, table):
+    """Each scene with its automatic key table and with a grid table wherever
+    the allowance reaches (most of these small scenes)."""
+    check_scene(oracle_mod, *random_scene(seed), table)
+
+
+@pytest.mark.parametrize("table", [1, 2])
+@pytest.mark.parametrize("seed", range(100, 108))
+def test_random_scene_fast_particles(gpu_lib, oracle_mod, seed, table):
+    """Speeds of ~150 (predictions 1-2 box lengths away at dt 1/120, many
+    cells beyond the walls): a grid table clamps those predictions onto its
+    edge cells, a bucket table wraps the cell index; both must still find
+    exactly the pairs within the cutoff."""
+    check_scene(oracle_mod, *random_scene(seed, speed=150.0), table)
+
+
+def check_scene(oracle_mod, p, pos, vel, dt, table):
     import fluidsim
-    p, pos, vel, dt = random_scene(seed)
     sim = fluidsim.FluidSimulation(p)
     sim.InitializeData(pos.shape[0], pos, vel)
+    sim.set_tuning(table=table)
     sim.debug_enable(True)
     sim.Update(dt, 1)
     got = sim.debug_export()
@@ -47,4 +64,4 @@ def test_random_scene_substep(gpu_lib, oracle_mod, seed):
     sim.close()
     opos, ovel, ref = oracle_mod.substep_f32(p, pos, vel, dt)
     fx = dict(ref, pos=opos, vel=ovel, bound=np.array(p.bound, np.float64))
-    print(seed, pos.shape[0], compare_substep(got, fx, dt, gpos, gvel))
+    print(pos.shape[0], table, compare_substep(got, fx, dt, gpos, gvel))
