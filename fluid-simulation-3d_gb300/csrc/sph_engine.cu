@@ -872,8 +872,8 @@ int Engine::SetTuning(const sph_tuning& t) {
   if (t.cell_tile != 1 && t.cell_tile != 64 && t.cell_tile != 128 &&
       t.cell_tile != 192 && t.cell_tile != 256)
     return Fail(SPH_ERR_INVALID, "cell_tile must be 1, 64, 128, 192 or 256");
-  if (t.gather != 2 && t.gather != 4 && t.gather != 8)
-    return Fail(SPH_ERR_INVALID, "gather must be 2, 4 or 8");
+  if (t.gather != 2 && t.gather != 3 && t.gather != 4 && t.gather != 8)
+    return Fail(SPH_ERR_INVALID, "gather must be 2, 3, 4 or 8");
   if (t.force_block != 0 &&
       (t.force_block < 32 || t.force_block > 1024 || (t.force_block & 31)))
     return Fail(SPH_ERR_INVALID, "force_block must be 0 or a multiple of 32 in [32, 1024]");
@@ -931,7 +931,7 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
       for (int fb : {64, 128, 256, 512})
         space.push_back(sph_tuning{win.block, win.cell_tile, 32, win.gather, fb, win.table});
     } else {
-      for (int g : {2, 4, 8})
+      for (int g : {2, 3, 4, 8})
         space.push_back(sph_tuning{win.block, win.cell_tile, 32, g, win.force_block, win.table});
     }
     for (const sph_tuning& t : space) {

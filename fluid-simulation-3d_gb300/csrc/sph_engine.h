@@ -160,7 +160,7 @@ class Engine {
   // Neighbour-list capacity per particle (pairs with dist <= r); a particle
   // with more neighbours is handled by the bucket walk in the force passes.
   static constexpr uint32_t kNbrCap = 64;
-  sph_tuning tuning_{128, 1, 32, 4, 0, 0};
+  sph_tuning tuning_{128, 1, 32, 2, 0, 0};
   int sm_count_ = 0;
 
   // The substep pipeline runs on an engine-owned non-blocking stream (stream

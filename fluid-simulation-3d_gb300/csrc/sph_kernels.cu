@@ -98,17 +98,20 @@ __device__ __forceinline__ void store_rec(float4* __restrict__ rec, uint32_t i,
                : "memory");
 }
 
-// kGather consecutive entries of slot i's list from entry k0. Each entry is
-// read once per pass, so the loads carry the streaming (evict-first) hint
-// and leave the cache to the neighbours' gathered state.
+// kGather consecutive entries of slot i's list from entry k0, those below
+// cnt (<= the list capacity) only: a batch of 3 that starts near the end of
+// a full list would otherwise read past the list rows. Each entry is read
+// once per pass, so the loads carry the streaming (evict-first) hint and
+// leave the cache to the neighbours' gathered state.
 template <int kGather>
 __device__ __forceinline__ void load_nbr_batch(const uint32_t* __restrict__ nbr,
                                                uint32_t i, uint32_t k0,
-                                               uint32_t stride,
+                                               uint32_t stride, uint32_t cnt,
                                                uint32_t (&j)[kGather]) {
   const uint32_t* p = nbr + nbr_index(i, k0, stride);
 #pragma unroll
-  for (int u = 0; u < kGather; ++u) j[u] = __ldcs(p + static_cast<uint64_t>(u) * stride);
+  for (int u = 0; u < kGather; ++u)
+    j[u] = k0 + u < cnt ? __ldcs(p + static_cast<uint64_t>(u) * stride) : 0u;
 }
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
@@ -763,8 +766,9 @@ __global__ void k_density(const uint2* __restrict__ tiles, uint32_t ntiles,
 // ---------------------------------------------------------------- pressure
 // CalculatePressureForce (:367-422) over the particle's neighbour list (self
 // excluded, dist <= r). shared/rho_j = 0.5*(Pi*(1/rho_j) + Pj/rho_j); the 0.5
-// is folded into ds2h/ds3h. The list is read four entries at a time so the
-// gathers of four neighbours are in flight together. A list that overflowed
+// is folded into ds2h/ds3h. The list is read kGather (2, 3, 4 or 8, tuned)
+// entries at a time so their neighbours' gathers are in flight together, the
+// next batch's entries loading meanwhile. A list that overflowed
 // falls back to the walk of the cell's runs.
 __device__ __forceinline__ void pressure_pair(const SceneDev& S, float3 p,
                                               float Pi, float Pni, float4 q,
@@ -818,14 +822,14 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
     const uint32_t cnt = ncount[i];
     if (cnt <= nbr_cap) {
       uint32_t jn[kGather];
-      if (cnt) load_nbr_batch<kGather>(nbr, i, 0, nbr_stride, jn);
+      if (cnt) load_nbr_batch<kGather>(nbr, i, 0, nbr_stride, cnt, jn);
       for (uint32_t k0 = 0; k0 < cnt; k0 += kGather) {
         uint32_t j[kGather];
         float4 q[kGather], b[kGather];
 #pragma unroll
         for (int u = 0; u < kGather; ++u) j[u] = (k0 + u < cnt) ? jn[u] : i;
         // the next batch's entries load while this batch's gathers fly
-        if (k0 + kGather < cnt) load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, jn);
+        if (k0 + kGather < cnt) load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, cnt, jn);
 #pragma unroll
         for (int u = 0; u < kGather; ++u) {
           q[u] = __ldg(pred + j[u]);
@@ -903,14 +907,14 @@ __global__ void k_visc_integrate(
       const uint32_t cnt = ncount[i];
       if (cnt <= nbr_cap) {
         uint32_t jn[kGather];
-        if (cnt) load_nbr_batch<kGather>(nbr, i, 0, nbr_stride, jn);
+        if (cnt) load_nbr_batch<kGather>(nbr, i, 0, nbr_stride, cnt, jn);
         for (uint32_t k0 = 0; k0 < cnt; k0 += kGather) {
           uint32_t j[kGather];
           float4 q[kGather], vj[kGather];
 #pragma unroll
           for (int u = 0; u < kGather; ++u) j[u] = (k0 + u < cnt) ? jn[u] : i;
           if (k0 + kGather < cnt)
-            load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, jn);
+            load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, cnt, jn);
 #pragma unroll
           for (int u = 0; u < kGather; ++u) load_rec(rec_v, j[u], q[u], vj[u]);
 #pragma unroll
@@ -1254,27 +1258,31 @@ cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
                     c.ncount, c.nbr_stride, c.nbr_cap);
 }
 
-// The instantiation for the launch's gather batch (2, 4, 8) and table forms,
-// from nine listed as (direct, buckets, mixed) x (2, 4, 8).
-template <class K>
-K pick_gather_tables(const LaunchCtx& c, K d2, K d4, K d8, K b2, K b4, K b8, K m2, K m4,
-                     K m8) {
-  const int g = c.gather == 2 ? 0 : c.gather == 8 ? 2 : 1;
-  const K direct[3] = {d2, d4, d8}, buckets[3] = {b2, b4, b8}, mixed[3] = {m2, m4, m8};
-  return c.tables == kTablesDirect    ? direct[g]
-         : c.tables == kTablesBuckets ? buckets[g]
-                                      : mixed[g];
+// The instantiations for a gather batch (2, 3, 4 or 8) and the launch's
+// table forms.
+template <int kTables>
+auto pressure_kernel(int gather) {
+  return gather == 2   ? k_pressure<2, kTables>
+         : gather == 3 ? k_pressure<3, kTables>
+         : gather == 8 ? k_pressure<8, kTables>
+                       : k_pressure<4, kTables>;
+}
+
+template <int kTables>
+auto visc_kernel(int gather) {
+  return gather == 2   ? k_visc_integrate<2, kTables>
+         : gather == 3 ? k_visc_integrate<3, kTables>
+         : gather == 8 ? k_visc_integrate<8, kTables>
+                       : k_visc_integrate<4, kTables>;
 }
 
 cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
                             cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_force;
-  auto kern = pick_gather_tables<decltype(&k_pressure<4, kTablesMixed>)>(
-      c, k_pressure<2, kTablesDirect>, k_pressure<4, kTablesDirect>, k_pressure<8, kTablesDirect>,
-      k_pressure<2, kTablesBuckets>, k_pressure<4, kTablesBuckets>,
-      k_pressure<8, kTablesBuckets>, k_pressure<2, kTablesMixed>, k_pressure<4, kTablesMixed>,
-      k_pressure<8, kTablesMixed>);
+  auto kern = c.tables == kTablesDirect    ? pressure_kernel<kTablesDirect>(c.gather)
+              : c.tables == kTablesBuckets ? pressure_kernel<kTablesBuckets>(c.gather)
+                                           : pressure_kernel<kTablesMixed>(c.gather);
   return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
                     tiles.n, c.scenes, c.pred, c.start, c.cell_first, c.cell_tab,
                     c.dens_a, c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap,
@@ -1286,12 +1294,9 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                                   cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_force;
-  auto kern = pick_gather_tables<decltype(&k_visc_integrate<4, kTablesMixed>)>(
-      c, k_visc_integrate<2, kTablesDirect>, k_visc_integrate<4, kTablesDirect>,
-      k_visc_integrate<8, kTablesDirect>, k_visc_integrate<2, kTablesBuckets>,
-      k_visc_integrate<4, kTablesBuckets>, k_visc_integrate<8, kTablesBuckets>,
-      k_visc_integrate<2, kTablesMixed>, k_visc_integrate<4, kTablesMixed>,
-      k_visc_integrate<8, kTablesMixed>);
+  auto kern = c.tables == kTablesDirect    ? visc_kernel<kTablesDirect>(c.gather)
+              : c.tables == kTablesBuckets ? visc_kernel<kTablesBuckets>(c.gather)
+                                           : visc_kernel<kTablesMixed>(c.gather);
   return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
                     tiles.n, c.scenes, c.pred, c.start, c.cell_first, c.cell_tab, c.nbr,
                     c.ncount, c.nbr_stride, c.nbr_cap, c.rec_v, c.pos2, c.vel2,

@@ -64,7 +64,7 @@ struct LaunchCtx {
   uint32_t* ncount = nullptr;   // neighbours per slot (> nbr_cap: overflow)
   uint32_t nbr_stride = 0;
   uint32_t nbr_cap = 0;
-  int gather = 4;               // neighbour entries gathered per batch (2, 4, 8)
+  int gather = 2;               // neighbour entries gathered per batch (2, 3, 4, 8)
   int cell_tile = 1;            // density-pass candidates held per cell tile
                                 // (1: thread-per-particle walk)
   int tables = kTablesMixed;    // key-table forms of the live scenes

@@ -253,7 +253,7 @@ class FluidSimulation:
     def kernel_launches(self) -> int:
         return int(self._lib.sph_kernel_launches(self._h))
 
-    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4,
+    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=2,
                    force_block=0, table=0):
         t = Tuning(block, cell_tile, particles_per_warp, gather, force_block, table)
         check(self._lib.sph_set_tuning(self._h, ctypes.byref(t)), self._h)
@@ -485,7 +485,7 @@ class Batch:
                                                _ptr(rgba), _ptr(depth), self._stream))
         return rgba, depth
 
-    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=4,
+    def set_tuning(self, block=128, cell_tile=1, particles_per_warp=32, gather=2,
                    force_block=0, table=0):
         t = Tuning(block, cell_tile, particles_per_warp, gather, force_block, table)
         self._check(self._lib.sph_batch_set_tuning(self._h, ctypes.byref(t)))

@@ -71,7 +71,7 @@ typedef struct sph_tuning {
                          of a cell in registers per pass                  */
   int32_t particles_per_warp; /* particles per warp: 32 (one per lane)    */
   int32_t gather;     /* neighbour-list entries whose gathers the force
-                         kernels issue together: 2, 4 or 8 (default 4)    */
+                         kernels issue together: 2, 3, 4 or 8 (default 2) */
   int32_t force_block; /* threads per block of the pressure and viscosity
                           kernels (multiple of 32, 32..1024); 0 = block   */
   int32_t table;      /* key table of the sort: 0 = one entry per cell of

@@ -112,7 +112,7 @@ def test_batch_autotune(gpu_lib):
     assert best["block"] in (64, 128, 256, 512)
     assert best["cell_tile"] in (1, 64, 128, 256)
     assert best["force_block"] in (0, 64, 128, 256, 512)  # 0: same as block
-    assert best["gather"] in (2, 4, 8)
+    assert best["gather"] in (2, 3, 4, 8)
     assert ms > 0.0
     assert b.tuning() == best
     # the sweep's trial steps leave no trace in the scenes' state
