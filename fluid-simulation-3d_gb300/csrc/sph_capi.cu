@@ -169,6 +169,14 @@ int sph_debug_export(sph_sim* sim, uint32_t* hash, uint32_t* key,
                               acc_p3, vel_p3, vel_v3, S(stream));
 }
 
+int sph_debug_export_layout(sph_sim* sim, uint32_t* cell, uint32_t* key,
+                            uint32_t* slot_ids, uint32_t* start, uint64_t start_cap,
+                            uint32_t* table_len, int* direct, void* stream) {
+  if (!sim) return SPH_ERR_INVALID;
+  return sim->eng.DebugExportLayout(sim->scene, cell, key, slot_ids, start, start_cap,
+                                    table_len, direct, S(stream));
+}
+
 int sph_status(sph_sim* sim, uint32_t* flags, void* stream) {
   if (!sim) return SPH_ERR_INVALID;
   return sim->eng.Status(flags, S(stream));

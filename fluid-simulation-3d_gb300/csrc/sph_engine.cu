@@ -491,6 +491,7 @@ int Engine::UploadScenes(int substeps, cudaStream_t st) {
     SPH_CUDA(cudaMemcpyAsync(d_scenes_, h.data(), sizeof(SceneDev) * hi,
                              cudaMemcpyHostToDevice, st), "upload scenes");
   SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  scene_dev_ = std::move(h);
   scenes_dirty_ = false;
   uploaded_substeps_ = substeps;
   return SPH_OK;
@@ -852,6 +853,38 @@ int Engine::DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
              "download densities");
     SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   }
+  return SPH_OK;
+}
+
+int Engine::DebugExportLayout(uint32_t id, uint32_t* cell, uint32_t* key,
+                              uint32_t* slot_ids, uint32_t* start, uint64_t start_cap,
+                              uint32_t* table_len, int* direct, cudaStream_t st) {
+  if (id >= max_scenes_ || !scenes_[id].live)
+    return Fail(SPH_ERR_INVALID, "no such scene");
+  if (!debug_valid_ || id >= scene_dev_.size()) return Fail(SPH_ERR_STATE, "no captured substep");
+  const SceneDev& d = scene_dev_[id];
+  const uint32_t n = scenes_[id].n;
+  const uint32_t b = old_base_[id];  // the captured substep's sorted slots
+  const uint64_t T = d.direct ? GridCells(d) : n;
+  if (table_len) *table_len = static_cast<uint32_t>(T);
+  if (direct) *direct = d.direct ? 1 : 0;
+  uint32_t* sc = static_cast<uint32_t*>(d_dbg_scratch_);  // 36 B per particle
+  SPH_CUDA(launch_export_layout(b, n, d_scenes_ + id, d_pos_[cur_], ctx_.pred, sc, sc + n,
+                                sc + 2ull * n, st), "layout export kernel");
+  auto d2h = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    if (!dst) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+  };
+  SPH_CUDA(d2h(cell, sc, 4ull * n), "download");
+  SPH_CUDA(d2h(key, sc + n, 4ull * n), "download");
+  SPH_CUDA(d2h(slot_ids, sc + 2ull * n, 4ull * n), "download");
+  if (start && start_cap >= T + 1) {
+    SPH_CUDA(cudaMemcpyAsync(start, ctx_.start + d.tbase, 4ull * (T + 1),
+                             cudaMemcpyDeviceToHost, st), "download start");
+  }
+  SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  if (start && start_cap >= T + 1)
+    for (uint64_t k = 0; k <= T; ++k) start[k] -= b;  // slot offsets in the scene
   return SPH_OK;
 }
 

@@ -59,6 +59,13 @@ class Engine {
   int DebugExport(uint32_t id, uint32_t* hash, uint32_t* key,
                   uint32_t* sorted_ids, uint32_t* start, float* dens2,
                   float* accp, float* velp, float* velv, cudaStream_t st);
+  // The timed sort's own layout of the captured substep (the internal cell
+  // index and key-table entry per particle, the particle at each slot, and
+  // the scene's key table as slot offsets, table_len + 1 entries); the
+  // table is copied only when start_cap holds it.
+  int DebugExportLayout(uint32_t id, uint32_t* cell, uint32_t* key, uint32_t* slot_ids,
+                        uint32_t* start, uint64_t start_cap, uint32_t* table_len,
+                        int* direct, cudaStream_t st);
   int Status(uint32_t* flags, cudaStream_t st);
 
   int SetTuning(const sph_tuning& t);
@@ -110,6 +117,7 @@ class Engine {
   std::vector<std::pair<uint64_t, uint64_t>> free_;
   uint32_t total_ = 0;              // live particles
   uint32_t table_total_ = 0;        // key-table entries of the live scenes
+  std::vector<SceneDev> scene_dev_;  // host copy of the uploaded scene table
   int tables_ = kTablesMixed;       // their forms (TableForms)
   bool layout_dirty_ = true;
   bool scenes_dirty_ = true;

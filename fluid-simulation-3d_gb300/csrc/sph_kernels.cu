@@ -1088,6 +1088,29 @@ __global__ void k_export_debug(uint32_t first, uint32_t n,
   ovelv[3 * id] = c.x; ovelv[3 * id + 1] = c.y; ovelv[3 * id + 2] = c.z;
 }
 
+// The timed sort's own layout of a captured substep, per slot of one scene:
+// the particle at each slot (slot_ids, slot order), and per particle (caller
+// order) its internal cell index (pred.w, written by k_reorder) and its
+// entry in the scene's key table.
+__global__ void k_export_layout(uint32_t first, uint32_t n,
+                                const SceneDev* __restrict__ scene,
+                                const float4* __restrict__ pos,
+                                const float4* __restrict__ pred,
+                                uint32_t* __restrict__ ocell,
+                                uint32_t* __restrict__ okey,
+                                uint32_t* __restrict__ oslot) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t s = first + k;
+  const uint32_t id = __float_as_uint(pos[s].w);
+  const uint32_t cell = __float_as_uint(pred[s].w);
+  oslot[k] = id;
+  if (id >= n) return;
+  const SceneDev& S = *scene;
+  ocell[id] = cell;
+  okey[id] = table_key(S, cell) - S.tbase;
+}
+
 // Load caller-order AoS arrays into a scene's slots (identity layout).
 __global__ void k_import(uint32_t first, uint32_t n,
                          const float* __restrict__ ipos,
@@ -1321,6 +1344,15 @@ cudaError_t launch_export_debug(uint32_t first, uint32_t n, const float4* pos,
   if (n == 0) return cudaSuccess;
   k_export_debug<<<(n + 255) / 256, 256, 0, st>>>(first, n, pos, accp, velp,
                                                   velv, oaccp, ovelp, ovelv);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export_layout(uint32_t first, uint32_t n, const SceneDev* scene,
+                                 const float4* pos, const float4* pred, uint32_t* ocell,
+                                 uint32_t* okey, uint32_t* oslot, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_export_layout<<<(n + 255) / 256, 256, 0, st>>>(first, n, scene, pos, pred, ocell,
+                                                  okey, oslot);
   return cudaGetLastError();
 }
 

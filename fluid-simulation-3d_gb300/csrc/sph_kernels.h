@@ -127,6 +127,13 @@ cudaError_t launch_export_debug(uint32_t first, uint32_t n, const float4* pos,
                                 const float4* accp, const float4* velp,
                                 const float4* velv, float* oaccp, float* ovelp,
                                 float* ovelv, cudaStream_t st);
+// The timed sort's layout of scene slots [first, first + n) after a
+// captured substep: caller index per slot (oslot[n]), and per caller index
+// the internal cell index (ocell[n]) and key-table entry relative to the
+// scene's table (okey[n]). All device pointers.
+cudaError_t launch_export_layout(uint32_t first, uint32_t n, const SceneDev* scene,
+                                 const float4* pos, const float4* pred, uint32_t* ocell,
+                                 uint32_t* okey, uint32_t* oslot, cudaStream_t st);
 // The reference's spatial lookup of the substep being launched (after its
 // sort): k_ref_hash, the scan, k_ref_scatter, k_ref_order into the dbg_*
 // buffers of `c`.

@@ -118,6 +118,8 @@ def _sig(L):
         "sph_batch_add_snapshot": (i, [_P, ctypes.c_char_p, ctypes.POINTER(u32), _P]),
         "sph_debug_enable": (i, [_P, i]),
         "sph_debug_export": (i, [_P] + [_P] * 8 + [_P]),
+        "sph_debug_export_layout": (i, [_P, _P, _P, _P, _P, u64, ctypes.POINTER(u32),
+                                        ctypes.POINTER(i), _P]),
         "sph_status": (i, [_P, ctypes.POINTER(u32), _P]),
         "sph_last_error": (ctypes.c_char_p, [_P]),
         "sph_global_error": (ctypes.c_char_p, []),

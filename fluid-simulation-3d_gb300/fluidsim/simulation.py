@@ -359,6 +359,26 @@ class FluidSimulation:
             _ptr(d["vel_v"]), self._stream), self._h)
         return d
 
+    def debug_export_layout(self):
+        """The timed sort's own layout of the captured substep
+        (sph_debug_export_layout): per particle its internal cell index and
+        key-table entry, the caller index at each slot, the key table's
+        start offsets and whether it is a grid table."""
+        n = self._n
+        tl, direct = ctypes.c_uint32(), ctypes.c_int()
+        d = dict(cell=np.empty(n, np.uint32), key=np.empty(n, np.uint32),
+                 slot_ids=np.empty(n, np.uint32))
+        check(self._lib.sph_debug_export_layout(
+            self._h, _ptr(d["cell"]), _ptr(d["key"]), _ptr(d["slot_ids"]), None, 0,
+            ctypes.byref(tl), ctypes.byref(direct), self._stream), self._h)
+        start = np.empty(tl.value + 1, np.uint32)
+        check(self._lib.sph_debug_export_layout(
+            self._h, None, None, None, _ptr(start), start.shape[0], None, None,
+            self._stream), self._h)
+        d["start"] = start
+        d["direct"] = bool(direct.value)
+        return d
+
     @property
     def num_particles(self):
         return self._n

@@ -189,6 +189,27 @@ int sph_debug_export(sph_sim *sim, uint32_t *hash, uint32_t *key,
                      float *acc_p3, float *vel_p3, float *vel_v3,
                      void *stream);
 
+/* The timed path's own spatial sort of the same captured substep (the
+ * layout every kernel of a substep reads; it replaces UpdateSpatialLookup,
+ * physicsWorld.cc:466-498, whose reference order sph_debug_export gives).
+ * Particles are sorted by an internal cell index: with the cell coordinates
+ * c = floor(pred / radius) and a grid of (gnx, gny, gnz) cells around the
+ * box, cell = cx' + cy' * gnx + cz' * gnx * gny (mod 2^32), where c' is c
+ * clamped to the grid (grid key table, one entry per cell: key = cell) or
+ * c minus the grid origin (bucket table, n entries: key = cell mod n). The
+ * order is stable by (key, cell, caller index), and start[k] is the slot of
+ * the first particle with key >= k (exclusive prefix of the key counts),
+ * start[table_len] = n. Outputs (host pointers, any may be NULL):
+ *   cell[n], key[n]   -- per particle, caller order;
+ *   slot_ids[n]       -- the caller index of the particle at each slot;
+ *   start[table_len+1] -- copied only when start_cap >= table_len + 1;
+ *   table_len, direct -- table entries, 1 for a grid table (0: buckets).
+ * Synchronises `stream`. */
+int sph_debug_export_layout(sph_sim *sim, uint32_t *cell, uint32_t *key,
+                            uint32_t *slot_ids, uint32_t *start,
+                            uint64_t start_cap, uint32_t *table_len,
+                            int *direct, void *stream);
+
 /* Device status flags OR-ed by kernels since the last call (cleared by the
  * read). Synchronises `stream`. */
 int sph_status(sph_sim *sim, uint32_t *flags, void *stream);

@@ -84,6 +84,9 @@ def lib():
         L.sph_oracle_subset_f64.argtypes = [
             ctypes.POINTER(OracleParams), ctypes.c_uint32, _P, ctypes.c_uint32,
             _P, ctypes.c_int, _P, _P, _P, _P, _P]
+        L.sph_oracle_subset_visc_f64.argtypes = [
+            ctypes.POINTER(OracleParams), ctypes.c_uint32, _P, _P, ctypes.c_uint32, _P,
+            ctypes.c_double, ctypes.c_int, _P, _P, _P]
         L.sph_oracle_hw_threads.restype = ctypes.c_int
         L.sph_oracle_render.argtypes = [_P, _P, ctypes.c_uint32, _P, _P, ctypes.c_uint32,
                                         ctypes.c_uint32, ctypes.c_float, _P, _P, _P]
@@ -177,6 +180,27 @@ def subset_f64(params, pred, subset, nthreads=0, with_abs=False):
     if rc != 0:
         raise ValueError(f"oracle subset failed: {rc}")
     return (dens, acc, absp, sens, dsens) if with_abs else (dens, acc)
+
+
+def subset_visc_f64(params, pred, velp, subset, dt, nthreads=0):
+    """FP64 Jacobi viscosity velocity increment of the listed particles from
+    FP32 predicted positions and post-pressure velocities (all n): returns
+    (dv [m, 3], sum|terms| [m], sensitivity to the distance [m])."""
+    pred = np.ascontiguousarray(pred, dtype=np.float32)
+    velp = np.ascontiguousarray(velp, dtype=np.float32)
+    subset = np.ascontiguousarray(subset, dtype=np.uint32)
+    m = subset.shape[0]
+    dv = np.empty((m, 3))
+    absv = np.empty(m)
+    dsens = np.empty(m)
+    prm = make_params(params)
+    rc = lib().sph_oracle_subset_visc_f64(ctypes.byref(prm), pred.shape[0], pred.ctypes.data,
+                                          velp.ctypes.data, m, subset.ctypes.data,
+                                          float(dt), nthreads, dv.ctypes.data,
+                                          absv.ctypes.data, dsens.ctypes.data)
+    if rc != 0:
+        raise ValueError(f"oracle viscosity subset failed: {rc}")
+    return dv, absv, dsens
 
 
 def hw_threads() -> int:

@@ -473,4 +473,53 @@ int sph_oracle_subset_f64(const oracle_params* p, uint32_t n, const float* pred,
   return 0;
 }
 
+int sph_oracle_subset_visc_f64(const oracle_params* p, uint32_t n, const float* pred,
+                               const float* velp, uint32_t m, const uint32_t* subset,
+                               double dt, int nthreads, double* out_dv, double* out_abs,
+                               double* out_dsens) {
+  if (!ParamsOk(p, n) || !pred || !velp || (m && !subset)) return -1;
+  for (uint32_t t = 0; t < m; ++t)
+    if (subset[t] >= n) return -2;
+  const Settings<double> S(p);
+  const KernelConsts<double> K(S.r);
+  std::vector<double> pd(pred, pred + 3 * static_cast<size_t>(n));
+  Lookup L;
+  std::vector<uint32_t> hashOf, keyOf;
+  BuildLookup(pd.data(), n, S.r, nthreads, L, hashOf, keyOf);
+  const double c = S.mu * dt;
+  ParallelFor(m, nthreads, [&](uint32_t t) {
+    const uint32_t i = subset[t];
+    const double* q0 = &pd[3 * i];
+    const double vix = velp[3 * i], viy = velp[3 * i + 1], viz = velp[3 * i + 2];
+    double fx = 0, fy = 0, fz = 0, absSum = 0, dsens = 0;
+    // CalculateViscosityForce, physicsWorld.cc:424-464, reading the
+    // post-pressure snapshot of every neighbour (Jacobi)
+    ForNeighbours(L, n, S.r, q0, [&](uint32_t j) {
+      if (j == i) return;
+      const double* q = &pd[3 * j];
+      const double sq = Dot3(q[0] - q0[0], q[1] - q0[1], q[2] - q0[2]);
+      if (sq > S.cut2) return;
+      const double infl = K.poly6(std::sqrt(sq));
+      const double ux = velp[3 * j] - vix, uy = velp[3 * j + 1] - viy,
+                   uz = velp[3 * j + 2] - viz;
+      fx += ux * infl; fy += uy * infl; fz += uz * infl;
+      const double du = std::sqrt(ux * ux + uy * uy + uz * uz);
+      absSum += du * infl;
+      // |d infl / d dist| = 6 dist (r^2 - dist^2)^2 * scale inside the support
+      if (sq < S.r * S.r) {
+        const double w = S.r * S.r - sq;
+        dsens += du * 6.0 * std::sqrt(sq) * w * w * K.vscale;
+      }
+    });
+    if (out_dv) {
+      out_dv[3 * t] = fx * c;
+      out_dv[3 * t + 1] = fy * c;
+      out_dv[3 * t + 2] = fz * c;
+    }
+    if (out_abs) out_abs[t] = absSum * std::fabs(c);
+    if (out_dsens) out_dsens[t] = dsens * std::fabs(c);
+  });
+  return 0;
+}
+
 }  // extern "C"

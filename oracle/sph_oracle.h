@@ -10,10 +10,11 @@
  * engine/physics/kernels.h:25-82 (smoothing kernels) of
  * Allkams/Fluid-Simulation-3D in plain C++ with the same float operation
  * order, so that, given the same sorted bucket order, it reproduces the
- * reference bit for bit in FP32 (pinned by tests/test_oracle_pin.py against
- * the reference itself compiled by oracle/Makefile).
+ * reference bit for bit in FP32 (pinned by tests/test_oracle_golden.py
+ * against fixtures the reference itself, compiled by oracle/Makefile,
+ * produced).
  *
- * Contract choices that the reference leaves open (documented in the design doc):
+ * Contract choices that the reference leaves open:
  *  - sorted order inside a key bucket is canonical: (key asc, index asc);
  *    the reference's std::sort is unstable (physicsWorld.cc:484);
  *  - the float->uint32 cell cast wraps modulo 2^32 ((uint32)(int32)c), the
@@ -100,6 +101,19 @@ int sph_oracle_subset_f64(const oracle_params *p, uint32_t n, const float *pred,
                           uint32_t m, const uint32_t *subset, int nthreads,
                           double *out_dens, double *out_acc, double *out_abs,
                           double *out_sens, double *out_dsens);
+
+/* FP64 Jacobi viscosity velocity increment (CalculateViscosityForce,
+ * physicsWorld.cc:424-464: mu * dt * sum over neighbours j != i of
+ * (v_j - v_i) * poly6(dist)) for the `m` listed particles of a scene whose
+ * FP32 predicted positions `pred` [3n] and post-pressure velocities `velp`
+ * [3n] are given (promoted to FP64; neighbours found by a fresh lookup).
+ * out_dv [3m]; out_abs [m] = mu * dt * sum of |term| (the scale of the
+ * sum); out_dsens [m] = mu * dt * sum of |d term / d dist| (what a rounding
+ * of the positions moves the increment by); any output may be NULL. */
+int sph_oracle_subset_visc_f64(const oracle_params *p, uint32_t n, const float *pred,
+                               const float *velp, uint32_t m, const uint32_t *subset,
+                               double dt, int nthreads, double *out_dv, double *out_abs,
+                               double *out_dsens);
 
 /* The headless render of sph_render (sph_render_oracle.cc): pos3/vel3 [3n]
  * in caller order, vp = ViewProj and proj = Projection (column-major),

@@ -1,8 +1,9 @@
 """The heavily non-uniform 8.4M-particle scene (two opposing 256x128x128
 blocks at spacing 0.08 in a 40x20x20 box, r 0.14, dt 1/240 in 2 substeps):
 after 1, 10 and 20 steps (the blocks meet and splash), one captured
-substep's density, near density and pressure acceleration against an FP64
-recomputation on a 65,536-particle random subset, reported per step.
+substep's density, near density, pressure acceleration and Jacobi viscosity
+velocity increment against an FP64 recomputation on a 65,536-particle
+random subset, reported per step.
 Tolerances: density 1e-4 relative; acceleration 1e-4 of the particle's sum
 of |pressure terms| (the sum cancels in the interior), plus
 the acceleration's own sensitivity to FP32 rounding of the densities:
@@ -13,7 +14,13 @@ and its sensitivity to the FP32 rounding of the distance: a spray particle
 whose only neighbour sits just inside the support has a term linear in
 r - dist, with r - dist as small as the rounding of dist itself, so an FP32
 dist (squared sum and square root, about 2 ulp of r) moves it by up to
-dsens * r * 2^-21 (dsens = sum of |d term / d dist| from the oracle)."""
+dsens * r * 2^-21 (dsens = sum of |d term / d dist| from the oracle).
+The viscosity increment (velocity after the viscosity pass minus the
+post-pressure velocity, physicsWorld.cc:424-464) is recomputed in FP64 from
+the GPU's own FP32 predicted positions and post-pressure velocities, which
+isolates the viscosity pass: |error| <= 1e-4 of mu * dt * sum|terms|, plus
+the rounding of the final FP32 sum v + dv (2^-22 |v|), plus the distance
+rounding term as above with the poly6 derivative."""
 import numpy as np
 import pytest
 
@@ -52,6 +59,20 @@ def check_against_fp64(oracle_mod, p, pos0, vel0, d, sub_dt, step):
           f"max err / bound {over.max():.3f}")
     assert drel.max() <= 1e-4
     assert np.all(da <= bound)
+    # viscosity pass: GPU's vel_v against vel_p + FP64 increment
+    dv64, absv, dsv = oracle_mod.subset_visc_f64(p, pred, d["vel_p"], subset, sub_dt)
+    vp = d["vel_p"][subset].astype(np.float64)
+    vv = d["vel_v"][subset].astype(np.float64)
+    ev = np.linalg.norm(vv - (vp + dv64), axis=1)
+    vbound = (1e-4 * absv + 2.0 ** -22 * np.linalg.norm(vv, axis=1) +
+              dsv * float(np.float32(p.radius)) * 2.0 ** -21)
+    vrel = ev / np.maximum(absv, 1e-30)
+    vover = np.where(vbound > 0, ev / np.where(vbound > 0, vbound, 1.0), 0.0)
+    print(f"step {step}: viscosity increment err / sum|terms| max {vrel.max():.3e} "
+          f"mean {vrel.mean():.3e} p99.9 {np.percentile(vrel, 99.9):.3e}; "
+          f"max err / bound {vover.max():.3f}; "
+          f"max |dv| {np.linalg.norm(dv64, axis=1).max():.3e}")
+    assert np.all(ev <= vbound)
 
 
 def test_opposing_blocks_8m_vs_fp64(gpu_lib, oracle_mod):

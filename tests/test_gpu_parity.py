@@ -206,3 +206,42 @@ def test_settings_surface_roundtrip(gpu_lib):
     assert sim.getDensity(10**6) == 0.0  # out of range -> 0 (physicsWorld.cc:163)
     assert sim.getDensity(0) > 0.0
     sim.close()
+
+
+@pytest.mark.parametrize("gather", [2, 3, 4, 8])
+@pytest.mark.parametrize("name", ["substep_dam_break_16k.npz", "substep_n2000_r0175.npz",
+                                  "substep_coincident.npz", "substep_single_cell.npz"])
+def test_substep_parity_gather(gpu_lib, name, gather):
+    """Every gather batch of the force kernels (the autotuner may pick any)
+    under the parity contract: predicated batch loads at the end of a list
+    and the padding of a partial batch."""
+    fx = load_fixture(name)
+    p = fixture_params(fx)
+    fx["bound"] = np.array(p.bound, np.float64)
+    got, pos, vel, dens = run_substep(fx, p, tuning=dict(gather=gather))
+    rep = compare_substep(got, fx, float(fx["dt"]), pos, vel)
+    print(name, gather, rep)
+
+
+@pytest.mark.parametrize("gather", [3, 4, 8])
+def test_full_lists_gather_bit_equal(gpu_lib, gather):
+    """A dense scene (r / spacing = 2.4, about 60 neighbours a particle, so
+    lists fill their 64 entries and some overflow to the walk) gives the
+    same bits under every gather batch as under batches of 2: the batch only
+    changes which loads are in flight, not the summation order."""
+    import fluidsim
+    from test_gpu_wide_lists import dense_scene
+    sc = dense_scene()
+    n = sc["pos"].shape[0]
+    outs = []
+    for g in (2, gather):
+        sim = fluidsim.FluidSimulation(sc["params"])
+        sim.InitializeData(n, sc["pos"], sc["vel"])
+        sim.set_tuning(gather=g)
+        for _ in range(2):
+            sim.Update(sc["dt"], 2)
+        assert sim.status() == 0
+        outs.append(sim.download())
+        sim.close()
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)

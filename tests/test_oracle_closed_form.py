@@ -106,3 +106,23 @@ def test_pair_beyond_radius_does_not_interact(oracle_mod):
         assert dbg["dens"][k, 0] == pytest.approx(w2(0.0, r), rel=RTOL)
         assert dbg["dens"][k, 1] == pytest.approx(w3(0.0, r), rel=RTOL)
         assert np.all(dbg["acc_p"][k] == 0.0)
+
+
+def test_subset_viscosity_f64_matches_reference_fp32():
+    """The FP64 viscosity evaluator the 8.4M test uses, fed the reference's
+    own FP32 predicted positions and post-pressure velocities of every
+    golden scene, reproduces the reference's FP32 post-viscosity velocity
+    within 1e-5 of the increment's sum of |terms| (plus the rounding of the
+    final sum and of the distances)."""
+    import oracle
+    from conftest import fixture_params, load_fixture, substep_fixtures
+    for name in substep_fixtures():
+        fx = load_fixture(name)
+        p = fixture_params(fx)
+        n = fx["pred"].shape[0]
+        dv, absv, dsens = oracle.subset_visc_f64(
+            p, fx["pred"], fx["vel_p"], np.arange(n, dtype=np.uint32), float(fx["dt"]))
+        err = np.linalg.norm(fx["vel_v"] - (fx["vel_p"].astype(np.float64) + dv), axis=1)
+        bound = (1e-5 * absv + 2.0 ** -22 * np.linalg.norm(fx["vel_v"], axis=1) +
+                 dsens * float(np.float32(p.radius)) * 2.0 ** -21)
+        assert np.all(err <= bound), name
