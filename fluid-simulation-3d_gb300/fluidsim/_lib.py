@@ -23,6 +23,7 @@ EXPORTS = (
     "sph_get_params", "sph_num_particles", "sph_upload", "sph_step",
     "sph_download", "sph_out_positions", "sph_upload_device",
     "sph_download_device", "sph_debug_enable", "sph_debug_export",
+    "sph_debug_export_layout",
     "sph_status", "sph_last_error", "sph_global_error", "sph_batch_create",
     "sph_batch_destroy", "sph_batch_add", "sph_batch_remove", "sph_batch_step",
     "sph_batch_download", "sph_batch_set_tuning", "sph_batch_get_tuning",
