@@ -14,6 +14,18 @@ API with the state in pinned host memory (upload + step + download every
 step). For N>1 every rank runs an independent replica of the scene (the path
 has no cross-scene exchange): weak scaling, max time over ranks.
 
+At N=1 the same line also carries the two other forms of one GPU:
+  "batched": 256 independent scenes (9.4M particles) advanced by one set of
+             segmented launches per substep, against the same scenes stepped
+             back to back as plain single-scene launches;
+  "served":  a Poisson stream of scene requests at 200 req/s for
+             --serve-seconds (default 60) through the library's serving loop
+             (HBM-budget admission, continuous batching), with p50/p99
+             per-step latency, against --serial-sample (default 100) of the
+             stream's requests run one after another as plain launches.
+--no-batched / --no-served leave them out; --workload batched_256 / served
+run one of them alone.
+
 --impl reference times the reference CPU implementation of the path on the
 host cores (the oracle's restatement, all hardware threads; the reference's
 own build where it exists here) on the same workload.
@@ -54,7 +66,10 @@ ALG_BYTES = {
     # (pred and velp travel together as the 32-byte rec_v record; its pred
     # half is a copy, so it is not counted as compulsory)
 }
-SURVEY_BYTES_PER_SUBSTEP = 300  # idealised whole-substep traffic per particle
+# Whole-substep compulsory traffic per particle: the sum of the per-kernel
+# algorithmic bytes of an idealised substep (predict+hash 68, counting sort
+# 20, reorder 68, density 24, forces 56, integrate 64).
+SUBSTEP_ALG_BYTES = 300
 
 
 def spatial_bytes(grid: bool, entries: int, n: int) -> float:
@@ -74,8 +89,12 @@ def parse():
     ap.add_argument("--workload", default="dam_break_1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--serve-seconds", type=float, default=1.0)
-    ap.add_argument("--serial-sample", type=int, default=12)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--serial-sample", type=int, default=100)
+    ap.add_argument("--no-batched", action="store_true",
+                    help="leave the batched (config 2) block out of the default line")
+    ap.add_argument("--no-served", action="store_true",
+                    help="leave the served (config 3) block out of the default line")
     ap.add_argument("--e2e-steps", type=int, default=None)
     return ap.parse_args()
 
@@ -502,8 +521,8 @@ def run_native(args):
                      "issue": ncu_issue(args.workload, dom)},
         "profiled_ms_per_step": prof_ms / args.steps,
         "substep": {"ms": sub_ms,
-                    "alg_GBps_at_300B": SURVEY_BYTES_PER_SUBSTEP * n / (sub_ms / 1000) / 1e9,
-                    "frac_at_300B": SURVEY_BYTES_PER_SUBSTEP * n / (sub_ms / 1000) / 1e9 / peak,
+                    "alg_GBps_at_300B": SUBSTEP_ALG_BYTES * n / (sub_ms / 1000) / 1e9,
+                    "frac_at_300B": SUBSTEP_ALG_BYTES * n / (sub_ms / 1000) / 1e9 / peak,
                     "phase_ms_per_launch": per_launch_ms, "phase_share": share,
                     "phase_roofline": phase_roofline},
         "e2e": {"value": e2e_value, "unit": UNIT, "steps": e2e_steps,
@@ -535,40 +554,50 @@ def run_native(args):
             "value": rate, "unit": UNIT, "cores": th, "kind": "port",
             "sample": f"{steps} full steps of the {n}-particle scene "
                       f"({steps * S} substeps), {el:.1f} s on {th} threads"}
+    if world == 1 and not args.no_batched:
+        # config 2, one GPU's form (each block samples its own clocks)
+        ck = ClockSampler(local)
+        ck.start()
+        line["batched"] = batched_block(args, stream)
+        line["batched"]["clocks"] = ck.stop()
+    if world == 1 and not args.no_served:
+        ck = ClockSampler(local)
+        ck.start()
+        line["served"] = served_block(args)
+        line["served"]["clocks"] = ck.stop()
     print(json.dumps(line), flush=True)
     if world > 1:
         tdist.destroy_process_group()
     return 0
 
 
-def run_batched(args):
-    """256 independent scenes (n log-uniform in [4096, 131072], box aspect
-    U[0.5,2], 20-60% fill, dt 1/60 in 3 substeps) advanced by one set of
-    segmented launches per substep, against the same scenes stepped back to
-    back as separate single-scene handles on the same stream."""
+def batched_block(args, stream):
+    """Config 2: 256 independent scenes (n log-uniform in [4096, 131072], box
+    aspect U[0.5,2], 20-60% fill, dt 1/60 in 3 substeps) advanced by one set
+    of segmented launches per substep (a captured graph per step), against
+    the same scenes stepped back to back as separate single-scene handles on
+    the same stream. Both time the same K steps from the scenes' initial
+    states, L2 flushed before each timed step."""
     import torch
 
     import fluidsim
     from fluidsim import scenes
 
-    rank, _, local = dist_env()
-    if rank != 0:  # one GPU's form: under torchrun rank 0 alone runs it
-        return 0
-    torch.cuda.set_device(local)
     scs = scenes.batched_scenes(256)
     total = sum(s["pos"].shape[0] for s in scs)
-    stream = torch.cuda.current_stream()
+    steps = args.steps
     b = fluidsim.Batch(total, 512, stream=stream)
-    ids = [b.add(s["params"], s["pos"], s["vel"], s["dt"]) for s in scs]
+    for s in scs:
+        b.add(s["params"], s["pos"], s["vel"], s["dt"])
     tuning, tuned_ms = b.autotune(3, steps_per_trial=1)
     for _ in range(args.warmup):
         b.step(3)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    e0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    e1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    e1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     launches0 = b.kernel_launches()
     torch.cuda.synchronize()
-    for k in range(args.steps):
+    for k in range(steps):
         flush.zero_()
         e0[k].record(stream)
         b.step(3)
@@ -588,7 +617,7 @@ def run_batched(args):
         for sim, s in zip(sims, scs):
             sim.step_async(s["dt"], 3)
     torch.cuda.synchronize()
-    for k in range(args.steps):
+    for k in range(steps):
         flush.zero_()
         e0[k].record(stream)
         for sim, s in zip(sims, scs):
@@ -598,70 +627,181 @@ def run_batched(args):
     pt = sum(a.elapsed_time(c) for a, c in zip(e0, e1)) / 1000.0
     for sim in sims:
         sim.close()
-    value = total * args.steps / bt
-    plain = total * args.steps / pt
-    print(json.dumps({
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * bt / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded scenes)",
-        "config": {"workload": "batched_256", "scenes": len(scs), "particles": total,
-                   "substeps": 3, "tuning": tuning, "autotune_ms": tuned_ms,
-                   "l2": "flushed (256 MiB write) before every timed step"},
-        "gpu_launches": int(launches),
-        "plain_back_to_back": {"value": plain, "ms_per_step": 1000 * pt / args.steps},
+    del flush
+    value = total * steps / bt
+    plain = total * steps / pt
+    return {
+        "workload": "batched_256", "scenes": len(scs), "particles": total,
+        "substeps": 3, "steps": steps, "warmup": args.warmup,
+        "value": value, "unit": UNIT, "ms_per_step": 1000 * bt / steps,
+        "gpu_launches": int(launches), "tuning": tuning, "autotune_ms": tuned_ms,
+        "plain_back_to_back": {"value": plain, "ms_per_step": 1000 * pt / steps},
         "batched_over_plain": value / plain,
-    }), flush=True)
-    return 0
+        "l2": "flushed (256 MiB write) before every timed step",
+        "timing": "CUDA events around each step on the library's stream"}
 
 
-def run_served(args):
-    """Poisson stream at 200 req/s for --serve-seconds; each request a dam
-    break or falling block of n log-uniform in [8192, 524288] particles for
-    K uniform in [60, 600] steps; admission by a 64 GB state budget. Reports
-    p50/p99 per-step latency and aggregate particle-steps/s, against the same
-    kind of requests run back to back as plain single-scene launches."""
+def served_requests(seconds, rate=200.0, seed=3):
+    """The request stream of config 3: Poisson arrivals at `rate` per second
+    for `seconds`; each request is (rid, arrival, seed of its scene). The
+    scene (fluidsim.scenes.request_scene: n log-uniform in [8192, 524288], K
+    uniform in [60, 600], dam break or falling block) is built from its seed
+    when it is needed, so the stream's ~12,000 requests are not held in host
+    memory at once."""
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            return out
+        out.append((len(out), t, int(rng.integers(1 << 62))))
+
+
+def request_of(desc):
+    from fluidsim import scenes
+    rid, arrival, seed = desc
+    sc = scenes.request_scene(np.random.default_rng(seed))
+    return rid, arrival, sc
+
+
+def served_block(args, budget=64 << 30, rate=200.0, server_queue=8):
+    """Config 3: the Poisson stream (200 req/s for --serve-seconds) through
+    the library's own serving loop (sph_server_*: continuous batching on a
+    worker thread, admission by the 64 GiB HBM budget). The client submits
+    each request once it has arrived and while the server holds fewer than
+    `server_queue` jobs waiting for admission (the rest wait, as built scenes
+    or not yet built, in arrival order), and collects finished jobs as they
+    complete. The measurement window is the stream itself: when its last
+    arrival time has passed, the server's statistics are read (particle-steps
+    run, per-step latency p50/p99 as the jobs saw it) and the jobs still
+    queued or resident are cancelled -- at 200 req/s the stream offers about
+    six times what one GPU serves, so a backlog remains, and it is reported.
+    The serial baseline runs the stream's first --serial-sample requests one
+    after another, each alone on its own single-scene handle (K steps)."""
+    import concurrent.futures as cf
+    import ctypes
+    import collections
+
+    from fluidsim import server
+
+    descs = served_requests(args.serve_seconds, rate)
+    srv = server.NativeServer(budget, max_scenes=8192, substeps=3)
+    lib, h = srv._lib, srv._h
+    pool = cf.ThreadPoolExecutor(4)
+    ahead = collections.deque()
+    nxt = 0
+    live = {}  # job -> (rid, n, K, arrival)
+    done_lat, done_work = [], 0
+    submitted = 0
+    t0 = time.perf_counter()
+    last_poll = 0.0
+    while True:
+        now = time.perf_counter() - t0
+        if now >= args.serve_seconds:
+            break
+        while len(ahead) < 32 and nxt < len(descs):
+            ahead.append(pool.submit(request_of, descs[nxt]))
+            nxt += 1
+        busy = False
+        if ahead and descs[submitted][1] <= now and srv.stats()["queued"] < server_queue:
+            rid, arrival, sc = ahead.popleft().result()
+            job = srv.submit(sc["params"], sc["pos"], sc["vel"], sc["dt"], sc["steps"])
+            live[job] = (rid, sc["pos"].shape[0], sc["steps"], arrival)
+            submitted += 1
+            busy = True
+        if now - last_poll > 0.05:
+            last_poll = now
+            for job in list(live):
+                if lib.sph_server_wait(h, job, None, None, None, ctypes.c_double(0.0)) == 0:
+                    rid, n, k, arrival = live.pop(job)
+                    done_lat.append(time.perf_counter() - t0 - arrival)
+                    done_work += n * k
+        if not busy:
+            time.sleep(0.001)
+    st = srv.stats()
+    for job in list(live):
+        srv.cancel(job)
+    srv.close()
+    pool.shutdown(wait=True, cancel_futures=True)
+    # offered load of the whole stream (n * K of every request)
+    from fluidsim import scenes
+    offered = sum(n * k for n, k in (scenes.request_size(np.random.default_rng(d[2]))
+                                     for d in descs)) / args.serve_seconds
+    # serial plain launches of the stream's first requests
+    t1 = time.perf_counter()
+    work = 0
+    for d in descs[: args.serial_sample]:
+        _, _, sc = request_of(d)
+        req = server.Request(d[0], sc["params"], sc["pos"], sc["vel"], sc["dt"],
+                             sc["substeps"], sc["steps"])
+        server.run_alone(req)
+        work += req.n * req.steps
+    serial_s = time.perf_counter() - t1
+    serial = work / serial_s
+    lat = np.asarray(done_lat) if done_lat else np.zeros(1)
+    rate_served = st["particle_steps_per_s"]
+    return {
+        "workload": "served", "rate_per_s": rate, "seconds": args.serve_seconds,
+        "requests_arrived": len(descs), "requests_submitted": submitted,
+        "requests_completed": len(done_lat), "requests_cancelled_at_end": len(live),
+        "budget_bytes": budget, "capacity_particles": st["capacity_particles"],
+        "server": "sph_server (native loop on a worker thread), substeps 3",
+        "value": rate_served, "unit": UNIT, "offered_particle_steps_per_s": offered,
+        "p50_step_ms": st["p50_step_ms"], "p99_step_ms": st["p99_step_ms"],
+        "batched_steps": st["steps"], "particle_steps": st["particle_steps"],
+        "wall_s": st["wall_s"],
+        "worker_s": {"in_steps": st["step_s"], "admitting": st["admit_s"],
+                     "retiring": st["retire_s"],
+                     "note": "admission staging overlaps the step it follows"},
+        "completion_s_p50": float(np.percentile(lat, 50)),
+        "completion_s_p99": float(np.percentile(lat, 99)),
+        "serial_plain": {"value": serial, "sample_requests": args.serial_sample,
+                         "seconds": serial_s,
+                         "how": "each request alone on its own single-scene handle, "
+                                "K steps, one after another"},
+        "served_over_serial": rate_served / serial,
+        "timing": "wall clock: the server's first admission to the end of its last "
+                  "step inside the window (sph_server_get_stats)"}
+
+
+def run_batched(args):
+    """--workload batched_256: the batched block alone, as its own line."""
     import torch
-
-    from fluidsim import scenes, server
 
     rank, _, local = dist_env()
     if rank != 0:  # one GPU's form: under torchrun rank 0 alone runs it
         return 0
     torch.cuda.set_device(local)
-    rng = np.random.default_rng(3)
-    reqs, t = [], 0.0
-    while True:
-        t += rng.exponential(1.0 / 200.0)
-        if t > args.serve_seconds:
-            break
-        sc = scenes.request_scene(rng)
-        reqs.append(server.Request(len(reqs), sc["params"], sc["pos"], sc["vel"],
-                                   sc["dt"], sc["substeps"], sc["steps"], arrival=t))
-    # the library's own serving loop (sph_server_*, a C++ worker thread)
-    srv = server.NativeServer(64 << 30, max_scenes=8192, substeps=reqs[0].substeps)
-    done, stats = srv.run(reqs, realtime=True)
-    srv.close()
-    # serial plain launches on a sample of the same stream
-    sample = reqs[: min(len(reqs), args.serial_sample)]
-    t0 = time.perf_counter()
-    work = 0
-    for r in sample:
-        server.run_alone(r)
-        work += r.n * r.steps
-    serial = work / (time.perf_counter() - t0)
+    blk = batched_block(args, torch.cuda.current_stream())
     print(json.dumps({
-        "metric": METRIC, "value": stats["particle_steps_per_s"], "unit": UNIT,
+        "metric": METRIC, "value": blk["value"], "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": blk["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded scenes)",
+        "config": {"workload": "batched_256", "scenes": blk["scenes"],
+                   "particles": blk["particles"], "substeps": 3,
+                   "tuning": blk["tuning"], "l2": blk["l2"]},
+        "gpu_launches": blk["gpu_launches"], "batched": blk}), flush=True)
+    return 0
+
+
+def run_served(args):
+    """--workload served: the served block alone, as its own line."""
+    import torch
+
+    rank, _, local = dist_env()
+    if rank != 0:  # one GPU's form: under torchrun rank 0 alone runs it
+        return 0
+    torch.cuda.set_device(local)
+    blk = served_block(args)
+    print(json.dumps({
+        "metric": METRIC, "value": blk["value"], "unit": UNIT,
         "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded request stream)",
-        "config": {"workload": "served", "rate_per_s": 200, "seconds": args.serve_seconds,
-                   "requests": len(reqs), "budget_bytes": 64 << 30,
-                   "server": "sph_server (native loop on a worker thread)"},
-        "p50_step_ms": stats["p50_step_ms"], "p99_step_ms": stats["p99_step_ms"],
-        "served": stats,
-        "serial_plain": {"value": serial, "sample_requests": len(sample)},
-        "served_over_serial": stats["particle_steps_per_s"] / serial,
-    }), flush=True)
+        "config": {"workload": "served", "rate_per_s": blk["rate_per_s"],
+                   "seconds": blk["seconds"], "budget_bytes": blk["budget_bytes"]},
+        "p50_step_ms": blk["p50_step_ms"], "p99_step_ms": blk["p99_step_ms"],
+        "served": blk}), flush=True)
     return 0
 
 

@@ -9,6 +9,7 @@
 // for bit: a batched step runs every particle's arithmetic in the same order
 // as a single-scene step.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -35,7 +36,9 @@ struct Job {
   uint32_t steps_left = 0;
   std::vector<float> pos, vel, dens;  // inputs, then the results
   uint32_t scene = 0;
-  bool resident = false, done = false, cancel = false;
+  bool resident = false, done = false;
+  std::atomic<bool> cancel{false};  // set under mu, read by the worker outside it
+  bool admitting = false;  // the worker is loading its inputs (outside mu)
   int status = SPH_OK;  // SPH_OK, or why the job ended without a result
   std::string why;
 };
@@ -92,6 +95,7 @@ struct sph_server {
   // statistics (under mu)
   uint64_t submitted = 0, completed = 0, cancelled = 0, failed = 0;
   uint64_t steps = 0, particle_steps = 0;
+  double step_s = 0, admit_s = 0, retire_s = 0;  // worker time per activity
   LatencyHistogram step_ms;  // each step weighted by the jobs it advanced
   bool started = false;
   Clock::time_point t_first{}, t_last{};
@@ -109,15 +113,26 @@ struct sph_server {
     } else {
       if (j->cancel) ++cancelled;
       else ++failed;
-      std::vector<float>().swap(j->pos);
-      std::vector<float>().swap(j->vel);
+      if (!j->admitting) {  // else the worker still reads the inputs
+        std::vector<float>().swap(j->pos);
+        std::vector<float>().swap(j->vel);
+      }
     }
     done_cv.notify_all();
   }
 
-  // Admission and cancellation of resident jobs; called by the worker with
-  // mu held.
-  void Admit() {
+  // One round of the worker, entered and left with mu held (lk). The engine
+  // is only touched by the worker and never under mu, so submitters,
+  // cancellers and waiters are not held up by device calls:
+  //   1. resident jobs cancelled since the last round leave the engine;
+  //   2. the resident jobs advance one batched step (launched, not waited
+  //      for), and meanwhile the waiting jobs are admitted in order while
+  //      the budget has room (a later, smaller job may backfill): their
+  //      inputs are staged and their uploads queued behind the step, so the
+  //      host work of admission overlaps the step on the device;
+  //   3. after the step completes, jobs at their last step are read back
+  //      and retired.
+  void Round(std::unique_lock<std::mutex>& lk) {
     for (auto it = resident.begin(); it != resident.end();) {
       if (it->second->cancel) {
         eng.RemoveScene(it->first);
@@ -127,35 +142,107 @@ struct sph_server {
         ++it;
       }
     }
-    for (auto it = waiting.begin(); it != waiting.end();) {
-      const std::shared_ptr<Job>& j = *it;
-      uint32_t sid = 0;
-      const int rc = eng.AddScene(j->prm, j->n, j->pos.data(),
-                                  j->vel.empty() ? nullptr : j->vel.data(), false, j->dt,
-                                  &sid, stream);
-      if (rc == SPH_ERR_NOMEM) {  // no room now; a smaller later job may fit
-        ++it;
+    std::vector<std::pair<uint32_t, std::shared_ptr<Job>>> stepped(resident.begin(),
+                                                                   resident.end());
+    uint64_t live = 0;
+    for (auto& kv : stepped) live += kv.second->n;
+    std::vector<std::shared_ptr<Job>> trying(waiting.begin(), waiting.end());
+    for (auto& j : trying) j->admitting = true;
+    lk.unlock();
+
+    const Clock::time_point t0 = Clock::now();
+    int rc = SPH_OK;
+    if (!stepped.empty()) rc = eng.Step(substeps, stream);
+    const Clock::time_point ta = Clock::now();
+    std::vector<int> arc(trying.size(), SPH_ERR_NOMEM);
+    std::vector<uint32_t> sids(trying.size(), 0);
+    if (rc == SPH_OK) {
+      for (size_t k = 0; k < trying.size(); ++k) {
+        const Job& j = *trying[k];
+        if (j.cancel) continue;  // cancelled before its turn
+        arc[k] = eng.AddScene(j.prm, j.n, j.pos.data(), j.vel.empty() ? nullptr : j.vel.data(),
+                              false, j.dt, &sids[k], stream);
+      }
+    }
+    const Clock::time_point tb = Clock::now();
+    if (rc == SPH_OK && cudaStreamSynchronize(stream) != cudaSuccess) rc = SPH_ERR_CUDA;
+    const Clock::time_point t1 = Clock::now();
+    const std::string eerr = rc == SPH_OK ? std::string() : std::string(eng.LastError());
+
+    lk.lock();
+    admit_s += Seconds(ta, tb);
+    bool admitted_any = false;
+    for (size_t k = 0; k < trying.size(); ++k) {
+      const std::shared_ptr<Job>& j = trying[k];
+      j->admitting = false;
+      if (j->done) {  // cancelled while being admitted
+        if (arc[k] == SPH_OK) eng.RemoveScene(sids[k]);
+        std::vector<float>().swap(j->pos);
+        std::vector<float>().swap(j->vel);
         continue;
       }
-      if (rc != SPH_OK) {
-        Finish(j, rc, eng.LastError());
-      } else {
-        j->scene = sid;
-        j->resident = true;
-        std::vector<float>().swap(j->pos);  // on the device now; results reuse them
-        std::vector<float>().swap(j->vel);
-        resident[sid] = j;
-        if (!started) {
-          started = true;
-          t_first = Clock::now();
-        }
+      if (j->cancel) continue;  // finished by cancel() already
+      if (arc[k] == SPH_ERR_NOMEM) continue;  // no room now; stays in the queue
+      waiting.erase(std::remove(waiting.begin(), waiting.end(), j), waiting.end());
+      if (arc[k] != SPH_OK) {
+        Finish(j, arc[k], eng.LastError());
+        continue;
       }
-      it = waiting.erase(it);
+      admitted_any = true;
+      j->scene = sids[k];
+      j->resident = true;
+      std::vector<float>().swap(j->pos);  // on the device now; results reuse them
+      std::vector<float>().swap(j->vel);
+      resident[sids[k]] = j;
+      if (!started) {
+        started = true;
+        t_first = t0;
+      }
     }
-    if (resident.empty() && !waiting.empty()) {
-      // nothing runs and nothing fits: these jobs can never be admitted
-      for (auto& j : waiting) Finish(j, SPH_ERR_NOMEM, "job does not fit the server's budget");
-      waiting.clear();
+    if (stepped.empty()) {
+      if (!admitted_any && resident.empty() && !waiting.empty()) {
+        // nothing runs and nothing fits: these jobs can never be admitted
+        for (auto& j : waiting) Finish(j, SPH_ERR_NOMEM, "job does not fit the server's budget");
+        waiting.clear();
+      }
+      return;
+    }
+    if (rc != SPH_OK) {
+      err = eerr;
+      for (auto& kv : resident) {
+        eng.RemoveScene(kv.first);
+        Finish(kv.second, rc, err);
+      }
+      resident.clear();
+      return;
+    }
+    ++steps;
+    particle_steps += live;
+    step_s += Seconds(t0, t1);
+    step_ms.Add(1000.0 * Seconds(t0, t1), static_cast<uint32_t>(stepped.size()));
+    t_last = t1;
+    std::vector<std::pair<uint32_t, std::shared_ptr<Job>>> retiring;
+    for (auto& kv : stepped)
+      if (--kv.second->steps_left == 0) retiring.push_back(kv);
+    if (retiring.empty()) return;
+    lk.unlock();
+    const Clock::time_point r0 = Clock::now();
+    std::vector<int> drc(retiring.size());
+    for (size_t k = 0; k < retiring.size(); ++k) {
+      Job& j = *retiring[k].second;
+      j.pos.resize(3ull * j.n);
+      j.vel.resize(3ull * j.n);
+      j.dens.resize(2ull * j.n);
+      drc[k] = eng.Download(retiring[k].first, j.pos.data(), j.vel.data(), j.dens.data(),
+                            false, stream);
+    }
+    const Clock::time_point r1 = Clock::now();
+    lk.lock();
+    retire_s += Seconds(r0, r1);
+    for (size_t k = 0; k < retiring.size(); ++k) {
+      eng.RemoveScene(retiring[k].first);
+      resident.erase(retiring[k].first);
+      Finish(retiring[k].second, drc[k], drc[k] == SPH_OK ? "" : eng.LastError());
     }
   }
 
@@ -171,45 +258,7 @@ struct sph_server {
         resident.clear();
         break;
       }
-      Admit();
-      if (resident.empty()) continue;
-      uint64_t live = 0;
-      for (auto& kv : resident) live += kv.second->n;
-      const uint32_t nres = static_cast<uint32_t>(resident.size());
-      lk.unlock();  // submitters and waiters run while the step does
-      const Clock::time_point t0 = Clock::now();
-      int rc = eng.Step(substeps, stream);
-      if (rc == SPH_OK && cudaStreamSynchronize(stream) != cudaSuccess) rc = SPH_ERR_CUDA;
-      const Clock::time_point t1 = Clock::now();
-      lk.lock();
-      if (rc != SPH_OK) {
-        err = eng.LastError();
-        for (auto& kv : resident) {
-          eng.RemoveScene(kv.first);
-          Finish(kv.second, rc, err);
-        }
-        resident.clear();
-        continue;
-      }
-      ++steps;
-      particle_steps += live;
-      step_ms.Add(1000.0 * Seconds(t0, t1), nres);
-      t_last = t1;
-      for (auto it = resident.begin(); it != resident.end();) {
-        const std::shared_ptr<Job>& j = it->second;
-        if (--j->steps_left > 0) {
-          ++it;
-          continue;
-        }
-        j->pos.resize(3ull * j->n);
-        j->vel.resize(3ull * j->n);
-        j->dens.resize(2ull * j->n);
-        const int d = eng.Download(it->first, j->pos.data(), j->vel.data(), j->dens.data(),
-                                   false, stream);
-        eng.RemoveScene(it->first);
-        Finish(j, d, d == SPH_OK ? "" : eng.LastError());
-        it = resident.erase(it);
-      }
+      Round(lk);
     }
   }
 };
@@ -334,6 +383,9 @@ int sph_server_get_stats(sph_server* s, sph_server_stats* out) {
     out->p50_step_ms = s->step_ms.Percentile(0.50);
     out->p99_step_ms = s->step_ms.Percentile(0.99);
   }
+  out->step_s = s->step_s;
+  out->admit_s = s->admit_s;
+  out->retire_s = s->retire_s;
   return SPH_OK;
 }
 

@@ -80,7 +80,9 @@ class ServerStats(ctypes.Structure):
                 ("steps", ctypes.c_uint64), ("particle_steps", ctypes.c_uint64),
                 ("capacity_particles", ctypes.c_uint64), ("wall_s", ctypes.c_double),
                 ("particle_steps_per_s", ctypes.c_double),
-                ("p50_step_ms", ctypes.c_double), ("p99_step_ms", ctypes.c_double)]
+                ("p50_step_ms", ctypes.c_double), ("p99_step_ms", ctypes.c_double),
+                ("step_s", ctypes.c_double), ("admit_s", ctypes.c_double),
+                ("retire_s", ctypes.c_double)]
 
 
 _P = ctypes.c_void_p

@@ -187,14 +187,22 @@ def batched_scenes(count: int = 256, seed: int = 2, lo: int = 4096,
     return out
 
 
+def request_size(rng, lo: int = 8192, hi: int = 524288, kmin: int = 60,
+                 kmax: int = 600):
+    """(n, K) of a served request: the first two draws of request_scene, so a
+    request's size is known without building its scene."""
+    n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+    k = int(rng.integers(kmin, kmax + 1))
+    return n, k
+
+
 def request_scene(rng, lo: int = 8192, hi: int = 524288, kmin: int = 60,
                   kmax: int = 600):
     """One served request: n log-uniform in [lo, hi], K steps uniform in
     [kmin, kmax], a dam-break or a falling block (centre uniform in the upper
     half of the box, downward speed U[0, 3]); box aspect (1, 0.75, 1) at 30%
     fill; dam-break constants, r 0.35, dt 1/60 in 3 substeps."""
-    n = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
-    k = int(rng.integers(kmin, kmax + 1))
+    n, k = request_size(rng, lo, hi, kmin, kmax)
     layout = "dam" if rng.uniform() < 0.5 else "fall"
     v = float(rng.uniform(0.0, 3.0)) if layout == "fall" else 0.0
     pos, vel, bound = fill_box_scene(rng, n, 0.3, (1.0, 0.75, 1.0),

@@ -356,6 +356,10 @@ typedef struct sph_server_stats {
                                     every step weighted by the jobs it
                                     advanced; from a fixed log histogram of
                                     0.5%-wide bins (within 0.25%)            */
+  double step_s;   /* worker seconds from each step's launch to its end
+                      (the admission uploads of the round overlap it)     */
+  double admit_s;  /* of which: staging and queueing admitted jobs' inputs */
+  double retire_s; /* worker seconds reading finished jobs back           */
 } sph_server_stats;
 
 int sph_server_create(uint64_t budget_bytes, uint32_t max_scenes, int substeps,
