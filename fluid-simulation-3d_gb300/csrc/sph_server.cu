@@ -13,6 +13,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstring>
 #include <deque>
 #include <map>
 #include <memory>
@@ -100,6 +101,12 @@ struct sph_server {
   bool started = false;
   Clock::time_point t_first{}, t_last{};
   std::string err;
+  // pinned staging ring for admitted jobs' inputs (nullptr: not available)
+  char* stage = nullptr;
+  size_t stage_cap = 0;
+  static constexpr size_t kStageBytes = 256ull << 20;
+  static constexpr int kDeferred = 1;  // admission result: try next round
+  static size_t StageAlign(size_t b) { return (b + 255) & ~static_cast<size_t>(255); }
 
   sph_server(uint64_t capacity, uint32_t max_scenes, int ss)
       : eng(capacity, max_scenes), substeps(ss) {}
@@ -157,11 +164,37 @@ struct sph_server {
     std::vector<int> arc(trying.size(), SPH_ERR_NOMEM);
     std::vector<uint32_t> sids(trying.size(), 0);
     if (rc == SPH_OK) {
+      // Inputs go through the pinned staging ring: the engine's import kernel
+      // reads them from there on the stream, behind the step, while this
+      // thread moves on. (A pageable upload would block this thread until the
+      // stream reached it, i.e. until the step ends.) The ring is free again
+      // after the round's synchronisation. A job too large for the ring is
+      // uploaded from its own (pageable) arrays.
+      size_t off = 0;
       for (size_t k = 0; k < trying.size(); ++k) {
         const Job& j = *trying[k];
         if (j.cancel) continue;  // cancelled before its turn
-        arc[k] = eng.AddScene(j.prm, j.n, j.pos.data(), j.vel.empty() ? nullptr : j.vel.data(),
-                              false, j.dt, &sids[k], stream);
+        const float* pp = j.pos.data();
+        const float* vp = j.vel.empty() ? nullptr : j.vel.data();
+        const size_t bytes = 12ull * j.n;
+        const size_t need = StageAlign(bytes) * (vp ? 2 : 1);
+        const size_t off0 = off;
+        if (stage && need <= stage_cap) {
+          if (off + need > stage_cap) {
+            arc[k] = kDeferred;  // the ring is full this round
+            continue;
+          }
+          std::memcpy(stage + off, pp, bytes);
+          pp = reinterpret_cast<const float*>(stage + off);
+          off += StageAlign(bytes);
+          if (vp) {
+            std::memcpy(stage + off, vp, bytes);
+            vp = reinterpret_cast<const float*>(stage + off);
+            off += StageAlign(bytes);
+          }
+        }
+        arc[k] = eng.AddScene(j.prm, j.n, pp, vp, false, j.dt, &sids[k], stream);
+        if (arc[k] != SPH_OK) off = off0;
       }
     }
     const Clock::time_point tb = Clock::now();
@@ -182,7 +215,7 @@ struct sph_server {
         continue;
       }
       if (j->cancel) continue;  // finished by cancel() already
-      if (arc[k] == SPH_ERR_NOMEM) continue;  // no room now; stays in the queue
+      if (arc[k] == SPH_ERR_NOMEM || arc[k] == kDeferred) continue;  // stays in the queue
       waiting.erase(std::remove(waiting.begin(), waiting.end(), j), waiting.end());
       if (arc[k] != SPH_OK) {
         Finish(j, arc[k], eng.LastError());
@@ -201,9 +234,18 @@ struct sph_server {
     }
     if (stepped.empty()) {
       if (!admitted_any && resident.empty() && !waiting.empty()) {
-        // nothing runs and nothing fits: these jobs can never be admitted
-        for (auto& j : waiting) Finish(j, SPH_ERR_NOMEM, "job does not fit the server's budget");
-        waiting.clear();
+        // Nothing runs: a waiting job that did not fit an empty engine never
+        // will. Jobs submitted after this round's snapshot are tried first.
+        bool all_tried = true;
+        for (auto& j : waiting) {
+          const auto t = std::find(trying.begin(), trying.end(), j);
+          all_tried = all_tried && t != trying.end() &&
+                      arc[static_cast<size_t>(t - trying.begin())] == SPH_ERR_NOMEM;
+        }
+        if (all_tried) {
+          for (auto& j : waiting) Finish(j, SPH_ERR_NOMEM, "job does not fit the server's budget");
+          waiting.clear();
+        }
       }
       return;
     }
@@ -280,6 +322,13 @@ int sph_server_create(uint64_t budget_bytes, uint32_t max_scenes, int substeps,
     cudaGetLastError();
     return SPH_ERR_CUDA;
   }
+  if (cudaHostAlloc(reinterpret_cast<void**>(&s->stage), sph_server::kStageBytes,
+                    cudaHostAllocDefault) == cudaSuccess) {
+    s->stage_cap = sph_server::kStageBytes;
+  } else {
+    cudaGetLastError();  // uploads then go from the jobs' own arrays
+    s->stage = nullptr;
+  }
   sph_server* raw = s.get();
   raw->worker = std::thread([raw] { raw->Run(); });
   *out = s.release();
@@ -295,6 +344,7 @@ int sph_server_destroy(sph_server* s) {
   s->work_cv.notify_all();
   if (s->worker.joinable()) s->worker.join();
   if (s->stream) cudaStreamDestroy(s->stream);
+  if (s->stage) cudaFreeHost(s->stage);
   delete s;
   return SPH_OK;
 }
