@@ -578,12 +578,11 @@ __device__ __forceinline__ void density_store(const SceneDev& S, uint32_t i,
 }
 
 // Thread-per-particle form in one pass: each lane walks its cell's runs,
-// classifies every candidate (FMA estimate, exact d2 inside the 2e-6 band)
-// and accumulates the density and its list as it goes. Lanes of one cell
-// walk identical runs, so their loads coincide. The walk is issue-bound and
-// runs at 32 registers (64 warps per SM); the direct rows' arithmetic would
-// take it to 36 unless capped (with no spills; the mixed form spills a few
-// row values).
+// classifies every candidate on the reference's exact d2 and accumulates the
+// density and its list as it goes. Lanes of one cell walk identical runs, so
+// their loads coincide. The walk is issue-bound: the cutoff and radius sit
+// in registers for the whole walk, and the hit path is one short predicated
+// block, at 32 registers (64 warps per SM; 40 measured slower).
 template <int kTables>
 __global__ void __maxnreg__(32) k_density_walk(const uint2* __restrict__ tiles,
                                uint32_t ntiles,
@@ -610,25 +609,24 @@ __global__ void __maxnreg__(32) k_density_walk(const uint2* __restrict__ tiles,
     uint32_t cnt = 0;
     uint32_t* wp = nbr + i;  // next list entry (a bumped pointer is the
                              // cheapest append in the hit path)
+    // Pairs with dist <= r (d2 <= cut_le) enter the list; the density takes
+    // (r - dist)^2 and (r - dist)^3 of the same pairs: those with dist == r
+    // exactly, which the reference leaves out, add (r - sqrt(d2))^2, the
+    // square of a rounding error.
+    const float cut = S.cut_le, r = S.r;
     const uint32_t cf = kTables == kTablesDirect ? 0u : cell_first[i];
     walk_runs<kTables>(S, start, cell_tab, cf, __float_as_uint(me.w), pred, [&](uint32_t j, float4 q) {
-      const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-      const float d2f = dist2_fast(dx, dy, dz);
-      if (d2f <= S.cut_hi && j != i) {
-        bool in_lt = true, in_le = true;
-        if (d2f > S.cut_lo) {
-          const float d2 = dist2(dx, dy, dz);
-          in_lt = d2 <= S.cut_lt;
-          in_le = d2 <= S.cut_le;
+      const float d2 = dist2(q.x - p.x, q.y - p.y, q.z - p.z);
+      if (d2 <= cut && j != i) {
+        if (cnt < nbr_cap) {
+          *wp = j;
+          wp += nbr_stride;
         }
-        if (in_le) {
-          if (cnt < nbr_cap) {
-            *wp = j;
-            wp += nbr_stride;
-          }
-          ++cnt;
-        }
-        if (in_lt) density_pair(S, d2f, s2, s3);
+        ++cnt;
+        const float w = r - sqrt_approx(d2);
+        const float w2 = w * w;
+        s2 += w2;
+        s3 = fmaf(w2, w, s3);
       }
     });
     density_store(S, i, s2, s3, cnt, dens_a, dens_b, ncount);
