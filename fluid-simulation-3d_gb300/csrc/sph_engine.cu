@@ -505,6 +505,7 @@ int Engine::RunSubsteps(int substeps, cudaStream_t st, bool carry) {
   c.block_force = tuning_.force_block ? tuning_.force_block : tuning_.block;
   c.cell_tile = tuning_.cell_tile;
   c.gather = tuning_.gather;
+  c.lanes = 32 / tuning_.particles_per_warp;
   c.tables = tables_;
   c.pdl = !profile_;  // phase events between kernels need plain launches
   c.max_blocks = 0;
@@ -900,8 +901,8 @@ int Engine::Status(uint32_t* flags, cudaStream_t st) {
 int Engine::SetTuning(const sph_tuning& t) {
   if (t.block < 32 || t.block > 1024 || (t.block & 31))
     return Fail(SPH_ERR_INVALID, "block must be a multiple of 32 in [32, 1024]");
-  if (t.particles_per_warp != 32)
-    return Fail(SPH_ERR_INVALID, "particles_per_warp must be 32");
+  if (t.particles_per_warp != 32 && t.particles_per_warp != 16)
+    return Fail(SPH_ERR_INVALID, "particles_per_warp must be 32 or 16");
   if (t.cell_tile != 1 && t.cell_tile != 64 && t.cell_tile != 128 &&
       t.cell_tile != 192 && t.cell_tile != 256)
     return Fail(SPH_ERR_INVALID, "cell_tile must be 1, 64, 128, 192 or 256");
@@ -922,7 +923,8 @@ int Engine::SetTuning(const sph_tuning& t) {
 }
 
 // Coordinate search: block size x cell tile (all neighbour kernels), then
-// the block size of the force kernels alone, then their gather batch.
+// the block size of the force kernels alone, then their particles per warp x
+// gather batch.
 int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
                      float* best_ms, cudaStream_t st) {
   if (steps_per_trial < 1) return Fail(SPH_ERR_INVALID, "steps_per_trial >= 1");
@@ -948,24 +950,47 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
     saved.push_back(std::move(v));
   }
   SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  // On any failure the caller's tuning comes back (the guard), and the
+  // events are released whichever way the sweep ends.
+  struct TuningGuard {
+    Engine* eng;
+    sph_tuning orig;
+    bool armed = true;
+    ~TuningGuard() {
+      if (armed) eng->SetTuning(orig);
+    }
+  } guard{this, tuning_};
+  struct Events {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~Events() {
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    }
+  } ev;
   sph_tuning win = tuning_;
   float win_ms = std::numeric_limits<float>::infinity();
-  cudaEvent_t e0, e1;
-  SPH_CUDA(cudaEventCreate(&e0), "cudaEventCreate");
-  SPH_CUDA(cudaEventCreate(&e1), "cudaEventCreate");
+  SPH_CUDA(cudaEventCreate(&ev.e0), "cudaEventCreate");
+  SPH_CUDA(cudaEventCreate(&ev.e1), "cudaEventCreate");
+  cudaEvent_t e0 = ev.e0, e1 = ev.e1;
+  const int ppw0 = tuning_.particles_per_warp;
   int rc = SPH_OK;
   for (int round = 0; round < 3 && rc == SPH_OK; ++round) {
     std::vector<sph_tuning> space;
     if (round == 0) {
       for (int b : {64, 128, 256, 512})
         for (int tile : {1, 64, 128, 256})
-          space.push_back(sph_tuning{b, tile, 32, tuning_.gather, 0, tuning_.table});
+          space.push_back(sph_tuning{b, tile, ppw0, tuning_.gather, 0, tuning_.table});
     } else if (round == 1) {
       for (int fb : {64, 128, 256, 512})
-        space.push_back(sph_tuning{win.block, win.cell_tile, 32, win.gather, fb, win.table});
+        space.push_back(sph_tuning{win.block, win.cell_tile, win.particles_per_warp,
+                                   win.gather, fb, win.table});
     } else {
-      for (int g : {2, 3, 4, 8})
-        space.push_back(sph_tuning{win.block, win.cell_tile, 32, g, win.force_block, win.table});
+      // the force kernels' mapping: particles per warp (one or two lanes a
+      // particle) x gather batch
+      for (int ppw : {32, 16})
+        for (int g : {2, 3, 4, 8})
+          space.push_back(sph_tuning{win.block, win.cell_tile, ppw, g, win.force_block,
+                                     win.table});
     }
     for (const sph_tuning& t : space) {
       if ((rc = SetTuning(t)) != SPH_OK) break;
@@ -981,8 +1006,6 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
       if (ms < win_ms) { win_ms = ms; win = t; }
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   for (const Saved& v : saved) {
     // Load puts the scene back in caller order at its current base, where
     // the saved densities and OutPositions line up slot for slot.
@@ -998,6 +1021,7 @@ int Engine::Autotune(int substeps, int steps_per_trial, sph_tuning* best,
   }
   SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");  // host copies die here
   if (rc != SPH_OK) return rc;
+  guard.armed = false;
   rc = SetTuning(win);
   if (best) *best = win;
   if (best_ms) *best_ms = win_ms;

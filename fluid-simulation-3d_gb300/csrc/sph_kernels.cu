@@ -103,7 +103,9 @@ __device__ __forceinline__ void store_rec(float4* __restrict__ rec, uint32_t i,
 // a full list would otherwise read past the list rows. Each entry is read
 // once per pass, so the loads carry the streaming (evict-first) hint and
 // leave the cache to the neighbours' gathered state.
-template <int kGather>
+// With kStep = 2 (two lanes per particle) a lane reads every other entry:
+// k0, k0 + 2, ...
+template <int kGather, int kStep = 1>
 __device__ __forceinline__ void load_nbr_batch(const uint32_t* __restrict__ nbr,
                                                uint32_t i, uint32_t k0,
                                                uint32_t stride, uint32_t cnt,
@@ -111,7 +113,7 @@ __device__ __forceinline__ void load_nbr_batch(const uint32_t* __restrict__ nbr,
   const uint32_t* p = nbr + nbr_index(i, k0, stride);
 #pragma unroll
   for (int u = 0; u < kGather; ++u)
-    j[u] = k0 + u < cnt ? __ldcs(p + static_cast<uint64_t>(u) * stride) : 0u;
+    j[u] = k0 + kStep * u < cnt ? __ldcs(p + static_cast<uint64_t>(kStep * u) * stride) : 0u;
 }
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t x) {
@@ -790,7 +792,12 @@ __device__ __forceinline__ void pressure_pair(const SceneDev& S, float3 p,
 
 
 
-template <int kGather, int kTables>
+// kLanes lanes per particle (tuning.particles_per_warp = 32 / kLanes): a
+// warp takes its tile's 32 particles in kLanes passes of 32 / kLanes; lane
+// pair (l, l + 16) shares a particle, each summing every other list entry,
+// and one shuffle combines the halves. The sums then run in another order
+// than with one lane, so the two forms agree to rounding, not bit for bit.
+template <int kGather, int kTables, int kLanes>
 __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
                            const SceneDev* __restrict__ scenes,
                            const float4* __restrict__ pred,
@@ -805,54 +812,69 @@ __global__ void k_pressure(const uint2* __restrict__ tiles, uint32_t ntiles,
                            const float4* __restrict__ vel,
                            float4* __restrict__ rec_v,
                            float4* __restrict__ dbg_accp) {
+  static_assert(kLanes == 1 || kLanes == 2, "one or two lanes per particle");
   pdl_enter();
   const uint32_t lane = lane_id();
+  constexpr uint32_t kPer = 32 / kLanes;  // particles per pass
+  const uint32_t sub = lane / kPer;       // this lane's share of the list
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
     const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
-    if (lane >= tile_len(tile)) continue;
-    const uint32_t i = tile.y + lane;
-    const float4 pi = pred[i];
-    const float3 p = make_float3(pi.x, pi.y, pi.z);
-    const float2 di = dens_a[i];
-    const float Pi = (di.x - S.rho0) * S.k, Pni = di.y * S.kn;
-    float3 f = make_float3(0.0f, 0.0f, 0.0f);
-    const uint32_t cnt = ncount[i];
-    if (cnt <= nbr_cap) {
-      uint32_t jn[kGather];
-      if (cnt) load_nbr_batch<kGather>(nbr, i, 0, nbr_stride, cnt, jn);
-      for (uint32_t k0 = 0; k0 < cnt; k0 += kGather) {
-        uint32_t j[kGather];
-        float4 q[kGather], b[kGather];
+#pragma unroll 1
+    for (uint32_t h = 0; h < kLanes; ++h) {
+      const uint32_t li = h * kPer + lane % kPer;
+      if (kLanes == 1 && li >= tile_len(tile)) break;
+      const bool live = li < tile_len(tile);
+      const uint32_t i = tile.y + (live ? li : 0u);
+      const float4 pi = pred[i];
+      const float3 p = make_float3(pi.x, pi.y, pi.z);
+      const float2 di = dens_a[i];
+      const float Pi = (di.x - S.rho0) * S.k, Pni = di.y * S.kn;
+      float3 f = make_float3(0.0f, 0.0f, 0.0f);
+      const uint32_t cnt = live ? ncount[i] : 0u;
+      if (cnt <= nbr_cap) {
+        uint32_t jn[kGather];
+        if (sub < cnt) load_nbr_batch<kGather, kLanes>(nbr, i, sub, nbr_stride, cnt, jn);
+        for (uint32_t k0 = sub; k0 < cnt; k0 += kLanes * kGather) {
+          uint32_t j[kGather];
+          float4 q[kGather], b[kGather];
 #pragma unroll
-        for (int u = 0; u < kGather; ++u) j[u] = (k0 + u < cnt) ? jn[u] : i;
-        // the next batch's entries load while this batch's gathers fly
-        if (k0 + kGather < cnt) load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, cnt, jn);
+          for (int u = 0; u < kGather; ++u) j[u] = (k0 + kLanes * u < cnt) ? jn[u] : i;
+          // the next batch's entries load while this batch's gathers fly
+          if (k0 + kLanes * kGather < cnt)
+            load_nbr_batch<kGather, kLanes>(nbr, i, k0 + kLanes * kGather, nbr_stride, cnt, jn);
 #pragma unroll
-        for (int u = 0; u < kGather; ++u) {
-          q[u] = __ldg(pred + j[u]);
-          b[u] = __ldg(dens_b + j[u]);
+          for (int u = 0; u < kGather; ++u) {
+            q[u] = __ldg(pred + j[u]);
+            b[u] = __ldg(dens_b + j[u]);
+          }
+#pragma unroll
+          for (int u = 0; u < kGather; ++u)
+            if (k0 + kLanes * u < cnt) pressure_pair(S, p, Pi, Pni, q[u], b[u], f);
         }
-#pragma unroll
-        for (int u = 0; u < kGather; ++u)
-          if (k0 + u < cnt) pressure_pair(S, p, Pi, Pni, q[u], b[u], f);
+      } else if (sub == 0) {
+        walk_runs<kTables>(S, start, cell_tab, cell_first[i], __float_as_uint(pi.w), pred,
+                           [&](uint32_t j, float4 q) {
+          if (j == i) return;
+          const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
+          if (dist2(dx, dy, dz) <= S.cut_le)
+            pressure_pair(S, p, Pi, Pni, q, __ldg(dens_b + j), f);
+        });
       }
-    } else {
-      walk_runs<kTables>(S, start, cell_tab, cell_first[i], __float_as_uint(pi.w), pred,
-                         [&](uint32_t j, float4 q) {
-        if (j == i) return;
-        const float dx = q.x - p.x, dy = q.y - p.y, dz = q.z - p.z;
-        if (dist2(dx, dy, dz) <= S.cut_le)
-          pressure_pair(S, p, Pi, Pni, q, __ldg(dens_b + j), f);
-      });
+      if (kLanes == 2) {
+        f.x += __shfl_xor_sync(kFull, f.x, 16);
+        f.y += __shfl_xor_sync(kFull, f.y, 16);
+        f.z += __shfl_xor_sync(kFull, f.z, 16);
+      }
+      if (!live || sub != 0) continue;
+      const float inv_rho = 1.0f / di.x;
+      const float ax = f.x * inv_rho, ay = f.y * inv_rho, az = f.z * inv_rho;
+      const float4 v = vel[i];
+      // viscosity record rec_v[i] = (predicted position, post-pressure velocity)
+      store_rec(rec_v, i, pi,
+                make_float4(v.x + ax * S.dt, v.y + ay * S.dt, v.z + az * S.dt, 0.f));
+      if (dbg_accp) dbg_accp[i] = make_float4(ax, ay, az, 0.0f);
     }
-    const float inv_rho = 1.0f / di.x;
-    const float ax = f.x * inv_rho, ay = f.y * inv_rho, az = f.z * inv_rho;
-    const float4 v = vel[i];
-    // viscosity record rec_v[i] = (predicted position, post-pressure velocity)
-    store_rec(rec_v, i, pi,
-              make_float4(v.x + ax * S.dt, v.y + ay * S.dt, v.z + az * S.dt, 0.f));
-    if (dbg_accp) dbg_accp[i] = make_float4(ax, ay, az, 0.0f);
   }
 }
 
@@ -876,7 +898,8 @@ __device__ __forceinline__ void visc_pair(const SceneDev& S, float3 p,
   }
 }
 
-template <int kGather, int kTables>
+// kLanes lanes per particle as in k_pressure.
+template <int kGather, int kTables, int kLanes>
 __global__ void k_visc_integrate(
     const uint2* __restrict__ tiles, uint32_t ntiles,
     const SceneDev* __restrict__ scenes, const float4* __restrict__ pred,
@@ -888,72 +911,88 @@ __global__ void k_visc_integrate(
     float4* __restrict__ out4, int fuse_next, uint32_t* __restrict__ count,
     uint4* __restrict__ keyrank, float4* __restrict__ dbg_velv,
     uint32_t* status) {
+  static_assert(kLanes == 1 || kLanes == 2, "one or two lanes per particle");
   pdl_enter();
   const uint32_t lane = lane_id();
+  constexpr uint32_t kPer = 32 / kLanes;  // particles per pass
+  const uint32_t sub = lane / kPer;       // this lane's share of the list
   for (uint32_t t = warp_id_global(); t < ntiles; t += warps_total()) {
     const uint2 tile = tiles[t];
     const SceneDev S = scenes[tile_scene(tile)];  // registers, not reloads
-    const bool live = lane < tile_len(tile);
-    const uint32_t i = tile.y + lane;
-    bool bad = false;
-    uint32_t key = 0, cell = 0, id = 0;
-    if (live) {
+#pragma unroll 1
+    for (uint32_t h = 0; h < kLanes; ++h) {
+      const uint32_t li = h * kPer + lane % kPer;
+      const bool in_tile = li < tile_len(tile);
+      const bool live = in_tile && sub == 0;  // the lane that owns the particle
+      const uint32_t i = tile.y + (in_tile ? li : 0u);
+      bool bad = false;
+      uint32_t key = 0, cell = 0, id = 0;
       float4 pi, vi;
-      load_rec(rec_v, i, pi, vi);
-      const float3 p = make_float3(pi.x, pi.y, pi.z);
       float3 f = make_float3(0.0f, 0.0f, 0.0f);
-      const uint32_t cnt = ncount[i];
-      if (cnt <= nbr_cap) {
-        uint32_t jn[kGather];
-        if (cnt) load_nbr_batch<kGather>(nbr, i, 0, nbr_stride, cnt, jn);
-        for (uint32_t k0 = 0; k0 < cnt; k0 += kGather) {
-          uint32_t j[kGather];
-          float4 q[kGather], vj[kGather];
+      if (in_tile) {
+        load_rec(rec_v, i, pi, vi);
+        const float3 p = make_float3(pi.x, pi.y, pi.z);
+        const uint32_t cnt = ncount[i];
+        if (cnt <= nbr_cap) {
+          uint32_t jn[kGather];
+          if (sub < cnt) load_nbr_batch<kGather, kLanes>(nbr, i, sub, nbr_stride, cnt, jn);
+          for (uint32_t k0 = sub; k0 < cnt; k0 += kLanes * kGather) {
+            uint32_t j[kGather];
+            float4 q[kGather], vj[kGather];
 #pragma unroll
-          for (int u = 0; u < kGather; ++u) j[u] = (k0 + u < cnt) ? jn[u] : i;
-          if (k0 + kGather < cnt)
-            load_nbr_batch<kGather>(nbr, i, k0 + kGather, nbr_stride, cnt, jn);
+            for (int u = 0; u < kGather; ++u) j[u] = (k0 + kLanes * u < cnt) ? jn[u] : i;
+            if (k0 + kLanes * kGather < cnt)
+              load_nbr_batch<kGather, kLanes>(nbr, i, k0 + kLanes * kGather, nbr_stride, cnt,
+                                              jn);
 #pragma unroll
-          for (int u = 0; u < kGather; ++u) load_rec(rec_v, j[u], q[u], vj[u]);
+            for (int u = 0; u < kGather; ++u) load_rec(rec_v, j[u], q[u], vj[u]);
 #pragma unroll
-          for (int u = 0; u < kGather; ++u)
-            if (k0 + u < cnt) visc_pair(S, p, vi, q[u], vj[u], f);
+            for (int u = 0; u < kGather; ++u)
+              if (k0 + kLanes * u < cnt) visc_pair(S, p, vi, q[u], vj[u], f);
+          }
+        } else if (sub == 0) {
+          walk_runs<kTables>(S, start, cell_tab, cell_first[i], __float_as_uint(pi.w), pred,
+                             [&](uint32_t j, float4 q) {
+            if (j != i) visc_pair(S, p, vi, q, __ldg(rec_v + 2ull * j + 1), f);
+          });
         }
-      } else {
-        walk_runs<kTables>(S, start, cell_tab, cell_first[i], __float_as_uint(pi.w), pred,
-                           [&](uint32_t j, float4 q) {
-          if (j != i) visc_pair(S, p, vi, q, __ldg(rec_v + 2ull * j + 1), f);
-        });
       }
-      const float c = S.vscale * S.mu * S.dt;
-      float3 v = make_float3(vi.x + f.x * c, vi.y + f.y * c, vi.z + f.z * c);
-      if (dbg_velv) dbg_velv[i] = make_float4(v.x, v.y, v.z, 0.0f);
-      float4 x = pos[i];
-      x.x = __fadd_rn(x.x, __fmul_rn(v.x, S.dt));
-      x.y = __fadd_rn(x.y, __fmul_rn(v.y, S.dt));
-      x.z = __fadd_rn(x.z, __fmul_rn(v.z, S.dt));
-      // edgeDst = halfSize - |pos|; if <= 0 clamp to the wall and reflect.
-      if (S.hx - fabsf(x.x) <= 0.0f) { x.x = S.hx * copysign_or_zero(x.x); v.x *= S.ndamp; }
-      if (S.hy - fabsf(x.y) <= 0.0f) { x.y = S.hy * copysign_or_zero(x.y); v.y *= S.ndamp; }
-      if (S.hz - fabsf(x.z) <= 0.0f) { x.z = S.hz * copysign_or_zero(x.z); v.z *= S.ndamp; }
-      pos[i] = x;
-      const float4 v4 = make_float4(v.x, v.y, v.z, 0.0f);
-      vel[i] = v4;
-      bad = !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) &&
-              isfinite(v.x) && isfinite(v.y) && isfinite(v.z));
-      id = __float_as_uint(x.w);
-      if (out4) {
-        if (id < S.n) out4[S.base + id] = make_float4(x.x, x.y, x.z, 0.34f);
-        else bad = true;
+      if (kLanes == 2) {
+        f.x += __shfl_xor_sync(kFull, f.x, 16);
+        f.y += __shfl_xor_sync(kFull, f.y, 16);
+        f.z += __shfl_xor_sync(kFull, f.z, 16);
       }
-      // the grid constants are read here, not kept in registers through the loop
-      if (fuse_next) predict_key(scenes[tile_scene(tile)], x, v4, key, cell);
+      if (live) {
+        const float c = S.vscale * S.mu * S.dt;
+        float3 v = make_float3(vi.x + f.x * c, vi.y + f.y * c, vi.z + f.z * c);
+        if (dbg_velv) dbg_velv[i] = make_float4(v.x, v.y, v.z, 0.0f);
+        float4 x = pos[i];
+        x.x = __fadd_rn(x.x, __fmul_rn(v.x, S.dt));
+        x.y = __fadd_rn(x.y, __fmul_rn(v.y, S.dt));
+        x.z = __fadd_rn(x.z, __fmul_rn(v.z, S.dt));
+        // edgeDst = halfSize - |pos|; if <= 0 clamp to the wall and reflect.
+        if (S.hx - fabsf(x.x) <= 0.0f) { x.x = S.hx * copysign_or_zero(x.x); v.x *= S.ndamp; }
+        if (S.hy - fabsf(x.y) <= 0.0f) { x.y = S.hy * copysign_or_zero(x.y); v.y *= S.ndamp; }
+        if (S.hz - fabsf(x.z) <= 0.0f) { x.z = S.hz * copysign_or_zero(x.z); v.z *= S.ndamp; }
+        pos[i] = x;
+        const float4 v4 = make_float4(v.x, v.y, v.z, 0.0f);
+        vel[i] = v4;
+        bad = !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) &&
+                isfinite(v.x) && isfinite(v.y) && isfinite(v.z));
+        id = __float_as_uint(x.w);
+        if (out4) {
+          if (id < S.n) out4[S.base + id] = make_float4(x.x, x.y, x.z, 0.34f);
+          else bad = true;
+        }
+        // the grid constants are read here, not kept in registers through the loop
+        if (fuse_next) predict_key(scenes[tile_scene(tile)], x, v4, key, cell);
+      }
+      if (fuse_next) {
+        const uint32_t r = aggregated_rank(count, key, live);
+        if (live) keyrank[i] = make_uint4(key, r, cell, id);
+      }
+      if (__any_sync(kFull, bad) && lane == 0) flag(status, kStatusNonFinite);
     }
-    if (fuse_next) {
-      const uint32_t r = aggregated_rank(count, key, live);
-      if (live) keyrank[i] = make_uint4(key, r, cell, id);
-    }
-    if (__any_sync(kFull, bad) && lane == 0) flag(status, kStatusNonFinite);
   }
 }
 
@@ -1281,29 +1320,39 @@ cudaError_t launch_density(const LaunchCtx& c, const Tiles& tiles,
 
 // The instantiations for a gather batch (2, 3, 4 or 8) and the launch's
 // table forms.
-template <int kTables>
+template <int kTables, int kLanes>
 auto pressure_kernel(int gather) {
-  return gather == 2   ? k_pressure<2, kTables>
-         : gather == 3 ? k_pressure<3, kTables>
-         : gather == 8 ? k_pressure<8, kTables>
-                       : k_pressure<4, kTables>;
+  return gather == 2   ? k_pressure<2, kTables, kLanes>
+         : gather == 3 ? k_pressure<3, kTables, kLanes>
+         : gather == 8 ? k_pressure<8, kTables, kLanes>
+                       : k_pressure<4, kTables, kLanes>;
 }
 
 template <int kTables>
+auto pressure_kernel(int gather, int lanes) {
+  return lanes == 2 ? pressure_kernel<kTables, 2>(gather) : pressure_kernel<kTables, 1>(gather);
+}
+
+template <int kTables, int kLanes>
 auto visc_kernel(int gather) {
-  return gather == 2   ? k_visc_integrate<2, kTables>
-         : gather == 3 ? k_visc_integrate<3, kTables>
-         : gather == 8 ? k_visc_integrate<8, kTables>
-                       : k_visc_integrate<4, kTables>;
+  return gather == 2   ? k_visc_integrate<2, kTables, kLanes>
+         : gather == 3 ? k_visc_integrate<3, kTables, kLanes>
+         : gather == 8 ? k_visc_integrate<8, kTables, kLanes>
+                       : k_visc_integrate<4, kTables, kLanes>;
+}
+
+template <int kTables>
+auto visc_kernel(int gather, int lanes) {
+  return lanes == 2 ? visc_kernel<kTables, 2>(gather) : visc_kernel<kTables, 1>(gather);
 }
 
 cudaError_t launch_pressure(const LaunchCtx& c, const Tiles& tiles,
                             cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_force;
-  auto kern = c.tables == kTablesDirect    ? pressure_kernel<kTablesDirect>(c.gather)
-              : c.tables == kTablesBuckets ? pressure_kernel<kTablesBuckets>(c.gather)
-                                           : pressure_kernel<kTablesMixed>(c.gather);
+  auto kern = c.tables == kTablesDirect    ? pressure_kernel<kTablesDirect>(c.gather, c.lanes)
+              : c.tables == kTablesBuckets ? pressure_kernel<kTablesBuckets>(c.gather, c.lanes)
+                                           : pressure_kernel<kTablesMixed>(c.gather, c.lanes);
   return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
                     tiles.n, c.scenes, c.pred, c.start, c.cell_first, c.cell_tab,
                     c.dens_a, c.dens_b, c.nbr, c.ncount, c.nbr_stride, c.nbr_cap,
@@ -1315,9 +1364,9 @@ cudaError_t launch_visc_integrate(const LaunchCtx& c, const Tiles& tiles,
                                   cudaStream_t st) {
   if (tiles.n == 0) return cudaSuccess;
   const int b = c.block_force;
-  auto kern = c.tables == kTablesDirect    ? visc_kernel<kTablesDirect>(c.gather)
-              : c.tables == kTablesBuckets ? visc_kernel<kTablesBuckets>(c.gather)
-                                           : visc_kernel<kTablesMixed>(c.gather);
+  auto kern = c.tables == kTablesDirect    ? visc_kernel<kTablesDirect>(c.gather, c.lanes)
+              : c.tables == kTablesBuckets ? visc_kernel<kTablesBuckets>(c.gather, c.lanes)
+                                           : visc_kernel<kTablesMixed>(c.gather, c.lanes);
   return launch_pdl(c.pdl, kern, grid_for(tiles.n, b, c.max_blocks), b, st, tiles.d,
                     tiles.n, c.scenes, c.pred, c.start, c.cell_first, c.cell_tab, c.nbr,
                     c.ncount, c.nbr_stride, c.nbr_cap, c.rec_v, c.pos2, c.vel2,

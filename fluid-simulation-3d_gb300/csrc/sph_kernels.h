@@ -65,6 +65,8 @@ struct LaunchCtx {
   uint32_t nbr_stride = 0;
   uint32_t nbr_cap = 0;
   int gather = 2;               // neighbour entries gathered per batch (2, 3, 4, 8)
+  int lanes = 1;                // lanes per particle in the force kernels (1 or 2:
+                                // 32 or 16 particles per warp)
   int cell_tile = 1;            // density-pass candidates held per cell tile
                                 // (1: thread-per-particle walk)
   int tables = kTablesMixed;    // key-table forms of the live scenes

@@ -4,13 +4,15 @@
 //
 // Layout, little-endian (the byte order of every host this builds for):
 //   0   8  magic "SPHSNAP1"
-//   8   4  version (1)
+//   8   4  version (2)
 //  12   4  n, particles
 //  16  52  sph_params field by field: radius, cutoff_sq, target_density,
 //          pressure_mult, near_pressure_mult, viscosity, gravity_scale
 //          (float), gravity_on (int32), bound[3], damping, predict_dt (float)
 //  68   4  dt of the scene's steps (float)
-//  72   8  FNV-1a 64 of the payload
+//  72   8  FNV-1a 64 of header bytes 0-71 followed by the payload, so a
+//          damaged setting is refused like damaged state (version 1 files,
+//          whose checksum covers the payload alone, still load)
 //  80      payload: positions float[3n], velocities float[3n], densities
 //          float[2n] (density, near density), all in the caller's order
 // A loaded scene continues bit for bit as if it had never been saved: the
@@ -27,20 +29,27 @@ namespace sph {
 namespace {
 
 constexpr char kMagic[8] = {'S', 'P', 'H', 'S', 'N', 'A', 'P', '1'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
 constexpr size_t kHeader = 80;
+constexpr size_t kDigestAt = 72;  // header bytes before the digest
 
-uint64_t Fnv1a(const std::vector<float>& a, uint64_t h) {
-  const unsigned char* p = reinterpret_cast<const unsigned char*>(a.data());
-  for (size_t i = 0; i < a.size() * sizeof(float); ++i) {
+uint64_t Fnv1a(const unsigned char* p, size_t bytes, uint64_t h) {
+  for (size_t i = 0; i < bytes; ++i) {
     h ^= p[i];
     h *= 1099511628211ull;
   }
   return h;
 }
 
-uint64_t PayloadHash(const SceneSnapshot& s) {
+uint64_t Fnv1a(const std::vector<float>& a, uint64_t h) {
+  return Fnv1a(reinterpret_cast<const unsigned char*>(a.data()), a.size() * sizeof(float), h);
+}
+
+// The checksum of a version-2 file: header bytes 0-71, then the payload
+// (head == nullptr: the payload alone, as version 1 wrote it).
+uint64_t Digest(const unsigned char* head, const SceneSnapshot& s) {
   uint64_t h = 14695981039346656037ull;
+  if (head) h = Fnv1a(head, kDigestAt, h);
   h = Fnv1a(s.pos, h);
   h = Fnv1a(s.vel, h);
   return Fnv1a(s.dens, h);
@@ -91,7 +100,7 @@ int Engine::SaveSnapshot(uint32_t id, const char* path, cudaStream_t st) {
   const float f5[5] = {p.bound[0], p.bound[1], p.bound[2], p.damping, p.predict_dt};
   Put(head, f5, sizeof f5);
   Put(head, &s.dt, 4);
-  const uint64_t h = PayloadHash(s);
+  const uint64_t h = Digest(head.data(), s);
   Put(head, &h, 8);
   if (head.size() != kHeader) return Fail(SPH_ERR_INVALID, "snapshot header layout");
   std::unique_ptr<std::FILE, FileCloser> f(std::fopen(path, "wb"));
@@ -115,7 +124,8 @@ int Engine::ReadSnapshot(const char* path, SceneSnapshot* s) {
   uint32_t version, n;
   std::memcpy(&version, head + 8, 4);
   std::memcpy(&n, head + 12, 4);
-  if (version != kVersion) return Fail(SPH_ERR_INVALID, "unknown snapshot version");
+  if (version != 1 && version != kVersion)
+    return Fail(SPH_ERR_INVALID, "unknown snapshot version");
   if (n == 0 || n >= (1u << 24)) return Fail(SPH_ERR_INVALID, "snapshot size out of range");
   float f7[7], f5[5];
   sph_params& p = s->prm;
@@ -144,7 +154,8 @@ int Engine::ReadSnapshot(const char* path, SceneSnapshot* s) {
     if (std::fread(a->data(), sizeof(float), a->size(), f.get()) != a->size())
       return Fail(SPH_ERR_INVALID, "snapshot truncated (payload)");
   if (std::fgetc(f.get()) != EOF) return Fail(SPH_ERR_INVALID, "snapshot has trailing bytes");
-  if (PayloadHash(*s) != h) return Fail(SPH_ERR_INVALID, "snapshot checksum mismatch");
+  if (Digest(version == 1 ? nullptr : head, *s) != h)
+    return Fail(SPH_ERR_INVALID, "snapshot checksum mismatch");
   return SPH_OK;
 }
 

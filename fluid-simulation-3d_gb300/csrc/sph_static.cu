@@ -3,19 +3,19 @@
 // Some callers cannot allocate device memory: an interactive render loop
 // (like the reference's GL app) must not call cudaMalloc/cudaFree mid-frame
 // because they synchronise the whole device and stall the frame; engines that
-// own a fixed memory budget or a pool forbid allocations from plug-ins; and
-// code running inside another library's stream-ordered or captured region
-// cannot make an allocating call at all. sph_spatial_lookup_static serves
-// them: the caller passes its own device buffers for inputs and outputs, and
-// the working memory (histogram, offsets, cursors, bucketed indices) is the
-// file-scope array below, 16 B per particle for up to
-// SPH_STATIC_LOOKUP_MAX particles -- 1 MiB that every GPU loading this
+// own a fixed memory budget or a pool forbid allocations from plug-ins.
+// sph_spatial_lookup_static serves them: the caller passes its own device
+// buffers for inputs and outputs, and the working memory (histogram, offsets,
+// cursors) is the file-scope array below, 12 B per particle for up to
+// SPH_STATIC_LOOKUP_MAX particles -- 768 KiB that every GPU loading this
 // library keeps until the process exits.
 //
 // The entry point has no counterpart in the reference; it builds the same
 // lookup as the main path's sort (hash, key = hash % n, the canonical
 // (key, index) order, the start table with 0x7fffffff for empty keys), in one
-// single-block kernel.
+// single-block kernel whose work is linear in n whatever the keys: the
+// ordering is a stable scatter in index order, so a scene whose particles all
+// share one key costs what any other scene of its size does.
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -33,8 +33,8 @@ constexpr uint32_t kMax = SPH_STATIC_LOOKUP_MAX;
 constexpr int kThreads = 1024;
 constexpr int kMaxDevices = 64;
 
-// count | offset | cursor | bucketed ids, kMax entries each.
-__device__ __align__(256) uint32_t g_lookup_scratch[4 * kMax];
+// count | offset | cursor, kMax entries each.
+__device__ __align__(256) uint32_t g_lookup_scratch[3 * kMax];
 
 std::mutex g_mu;
 uint32_t* g_scratch_addr[kMaxDevices] = {};
@@ -77,7 +77,6 @@ k_lookup_static(const float* __restrict__ pred3, uint32_t n, float r,
   uint32_t* cnt = scratch;
   uint32_t* off = scratch + kMax;
   uint32_t* cur = scratch + 2 * kMax;
-  uint32_t* tmp = scratch + 3 * kMax;
   // The array keeps the previous call's contents: clear the histogram.
   for (uint32_t k = threadIdx.x; k < n; k += kThreads) cnt[k] = 0u;
   __syncthreads();
@@ -107,19 +106,30 @@ k_lookup_static(const float* __restrict__ pred3, uint32_t n, float r,
     carry += total;
   }
   __syncthreads();
-  // Bucket by arrival, then order each bucket by index.
-  for (uint32_t i = threadIdx.x; i < n; i += kThreads) {
-    const uint32_t s = atomicAdd(cur + okey[i], 1u);
-    tmp[s] = i;
-  }
-  __syncthreads();
-  for (uint32_t s = threadIdx.x; s < n; s += kThreads) {
-    const uint32_t id = tmp[s];
-    const uint32_t key = okey[id];
-    const uint32_t b0 = off[key], b1 = b0 + cnt[key];
-    uint32_t rank = 0;
-    for (uint32_t u = b0; u < b1; ++u) rank += tmp[u] < id ? 1u : 0u;
-    osorted[b0 + rank] = id;
+  // Stable scatter in index order: the first warp walks the particles 32 at
+  // a time; lanes with equal keys take consecutive slots of their bucket in
+  // lane (= index) order, from the bucket's cursor, which the leader of the
+  // equal-key lanes advances. n / 32 warp steps, whatever the keys.
+  if (threadIdx.x < 32) {
+    const uint32_t lane = threadIdx.x;
+    for (uint32_t base = 0; base < n; base += 32) {
+      const uint32_t i = base + lane;
+      const bool valid = i < n;
+      const uint32_t am = __ballot_sync(0xffffffffu, valid);
+      if (valid) {
+        const uint32_t key = okey[i];
+        const uint32_t peers = __match_any_sync(am, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t b = 0;
+        if (static_cast<int>(lane) == leader) {
+          b = cur[key];
+          cur[key] = b + __popc(peers);
+        }
+        b = __shfl_sync(peers, b, leader);
+        osorted[b + __popc(peers & ((1u << lane) - 1u))] = i;
+      }
+      __syncwarp();  // the cursors' updates are seen by the next step's leaders
+    }
   }
 }
 

@@ -23,14 +23,14 @@ def _fnv1a(data: bytes) -> int:
 
 def read(path, verify: bool = False) -> dict:
     """Returns dict(params=Params, dt, pos [n,3], vel [n,3], dens [n,2]).
-    verify: also check the payload checksum here (a byte loop in Python;
-    the library checks it whenever it loads a snapshot)."""
+    verify: also check the checksum here (a byte loop in Python; the
+    library checks it whenever it loads a snapshot)."""
     with open(path, "rb") as f:
         blob = f.read()
     if len(blob) < HEADER or blob[:8] != MAGIC:
         raise ValueError(f"{path}: not a snapshot")
     version, n = struct.unpack_from("<II", blob, 8)
-    if version != 1:
+    if version not in (1, 2):
         raise ValueError(f"{path}: unknown snapshot version {version}")
     if len(blob) != HEADER + 32 * n:
         raise ValueError(f"{path}: {len(blob)} bytes, expected {HEADER + 32 * n}")
@@ -39,7 +39,10 @@ def read(path, verify: bool = False) -> dict:
     f5 = struct.unpack_from("<5f", blob, 48)
     (dt,) = struct.unpack_from("<f", blob, 68)
     (digest,) = struct.unpack_from("<Q", blob, 72)
-    if verify and _fnv1a(blob[HEADER:]) != digest:
+    # version 2: the checksum covers header bytes 0-71 and the payload;
+    # version 1: the payload alone
+    covered = blob[HEADER:] if version == 1 else blob[:72] + blob[HEADER:]
+    if verify and _fnv1a(covered) != digest:
         raise ValueError(f"{path}: checksum mismatch")
     p = Params()
     (p.radius, p.cutoff_sq, p.target_density, p.pressure_mult, p.near_pressure_mult,

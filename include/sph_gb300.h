@@ -69,7 +69,10 @@ typedef struct sph_tuning {
                          its cell's runs (default); 64, 128, 192 or 256 =
                          warp-cooperative form holding that many candidates
                          of a cell in registers per pass                  */
-  int32_t particles_per_warp; /* particles per warp: 32 (one per lane)    */
+  int32_t particles_per_warp; /* pressure and viscosity kernels: 32 (one
+                         lane per particle, default) or 16 (two lanes per
+                         particle, each summing every other neighbour of
+                         its list; agrees with 32 to rounding)            */
   int32_t gather;     /* neighbour-list entries whose gathers the force
                          kernels issue together: 2, 3, 4 or 8 (default 2) */
   int32_t force_block; /* threads per block of the pressure and viscosity
@@ -227,7 +230,8 @@ int sph_phase_times(sph_sim *sim, double out_ms[6]);
 /* Kernel launch configuration of a single-scene handle, and its autotuner:
  * times real steps of dt/substeps (steps_per_trial per candidate, after one
  * untimed step) over the neighbour block size x cell tile, then the force
- * kernels' block size, then the gather batch; keeps the fastest and reports
+ * kernels' block size, then their particles per warp x gather batch; keeps
+ * the fastest and reports
  * it (best may be NULL) with its ms per step. The state (positions,
  * velocities, densities, OutPositions) is saved before the sweep and
  * restored after it. */
@@ -251,17 +255,17 @@ const char *sph_global_error(void);
  * reference: this is an extra entry point for callers that cannot allocate
  * device memory -- a render loop that must not stall a frame on cudaMalloc's
  * device-wide synchronisation, an engine that owns a fixed memory pool and
- * forbids plug-ins to allocate, code running inside another library's
- * captured or stream-ordered region.
+ * forbids plug-ins to allocate.
  *
  * Builds, for n predicted positions (device float[3n], the caller's
  * buffers), the same lookup as the main path: hash[n] and key[n] = hash % n
  * per particle, sorted_ids[n] in (key, index) order and start[n]
  * (0x7fffffff for an empty key) -- all device buffers of the caller. The
- * working memory is one array inside the library of 16 B per particle for
- * at most SPH_STATIC_LOOKUP_MAX particles (1 MiB, held on every GPU that
+ * working memory is one array inside the library of 12 B per particle for
+ * at most SPH_STATIC_LOOKUP_MAX particles (768 KiB, held on every GPU that
  * loads the library until the process exits); larger n is rejected with
- * SPH_ERR_INVALID. Nothing is allocated: no cudaMalloc/cudaFree or
+ * SPH_ERR_INVALID. The work is linear in n whatever the keys (particles
+ * that all share one key included). Nothing is allocated: no cudaMalloc/cudaFree or
  * allocating library call. The first call on a device resolves that array's
  * address (cudaGetSymbolAddress) with the device current, so make the first
  * call on each device before any stream capture. Each device has its own

@@ -114,3 +114,23 @@ def sort_layout(params, pred, table=0):
     start = np.zeros(table_len + 1, np.uint32)
     start[1:] = np.cumsum(counts, dtype=np.uint64).astype(np.uint32)
     return dict(cell=cell, key=key, slot_ids=slot_ids, start=start, direct=direct)
+
+
+def reference_lookup(pred, radius):
+    """The reference's own spatial lookup (UpdateSpatialLookup,
+    physicsWorld.cc:466-498) for predicted positions `pred`: HashCell of each
+    particle's cell (physicsWorld.cc:505-511, the float->uint32 cast wrapping
+    as on x86-64), key = hash % n, the (key, index) order, and startIndices
+    (0x7fffffff for an empty key)."""
+    n = pred.shape[0]
+    c = cell_coords(pred, radius) & U32
+    h = ((c[:, 0] * 15823 + c[:, 1] * 9737333 + c[:, 2] * 440817757) & U32).astype(np.uint32)
+    key = (h % np.uint32(n)).astype(np.uint32)
+    ids = np.arange(n, dtype=np.uint32)
+    order = ids[np.lexsort((ids, key))].astype(np.uint32)
+    start = np.full(n, 0x7FFFFFFF, np.uint32)
+    ks = key[order]
+    first = np.ones(n, bool)
+    first[1:] = ks[1:] != ks[:-1]
+    start[ks[first]] = np.nonzero(first)[0].astype(np.uint32)
+    return dict(hash=h, key=key, sorted_ids=order, start=start)

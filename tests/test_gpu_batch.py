@@ -113,6 +113,7 @@ def test_batch_autotune(gpu_lib):
     assert best["cell_tile"] in (1, 64, 128, 256)
     assert best["force_block"] in (0, 64, 128, 256, 512)  # 0: same as block
     assert best["gather"] in (2, 3, 4, 8)
+    assert best["particles_per_warp"] in (16, 32)
     assert ms > 0.0
     assert b.tuning() == best
     # the sweep's trial steps leave no trace in the scenes' state
@@ -251,3 +252,26 @@ def test_removed_scene_room_is_reused_before_the_next_step(gpu_lib):
         for g, r in zip(b.download(sid), alone(sc, 1)):
             assert np.array_equal(g, r), sid
     b.close()
+
+
+def test_batch_equals_alone_two_lanes_per_particle(gpu_lib):
+    """With 16 particles per warp (two lanes a particle in the force
+    kernels) a batch still equals each scene stepped alone bit for bit."""
+    import fluidsim
+    scs = small_scenes(3, seed=31)
+    b = fluidsim.Batch(sum(s["pos"].shape[0] for s in scs), 4)
+    b.set_tuning(particles_per_warp=16, gather=3)
+    ids = [b.add(s["params"], s["pos"], s["vel"], s["dt"]) for s in scs]
+    for _ in range(3):
+        b.step(3)
+    got = [b.download(i) for i in ids]
+    b.close()
+    for s, g in zip(scs, got):
+        sim = fluidsim.FluidSimulation(s["params"])
+        sim.InitializeData(s["pos"].shape[0], s["pos"], s["vel"])
+        sim.set_tuning(particles_per_warp=16, gather=3)
+        for _ in range(3):
+            sim.Update(s["dt"], 3)
+        for a, w in zip(g, sim.download()):
+            assert np.array_equal(a, w)
+        sim.close()

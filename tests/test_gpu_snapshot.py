@@ -56,7 +56,10 @@ def test_damaged_or_mismatched_snapshots_are_refused(gpu_lib, tmp_path):
     sim.save(f)
     blob = bytearray(f.read_bytes())
     cases = {"flip": bytes(blob[:1000] + bytes([blob[1000] ^ 1]) + blob[1001:]),
-             "short": bytes(blob[:-8]), "magic": b"X" + bytes(blob[1:])}
+             "short": bytes(blob[:-8]), "magic": b"X" + bytes(blob[1:]),
+             # a flipped bit of the radius (header byte 16): refused, not read
+             # as another plausible scene
+             "setting": bytes(blob[:16] + bytes([blob[16] ^ 1]) + blob[17:])}
     for name, data in cases.items():
         g = tmp_path / f"{name}.sph"
         g.write_bytes(data)

@@ -45,3 +45,15 @@ def test_layout_consistent(name, table):
         assert np.array_equal(L["key"], L["cell"])
     else:
         assert np.array_equal(L["key"], L["cell"] % np.uint32(n))
+
+
+@pytest.mark.parametrize("name", substep_fixtures())
+def test_reference_lookup_matches_reference(name):
+    """The numpy restatement of the reference's own lookup (hash, key,
+    (key, index) order, startIndices) reproduces the reference's outputs."""
+    from oracle import layout
+    fx = load_fixture(name)
+    p = fixture_params(fx)
+    L = layout.reference_lookup(fx["pred"], np.float32(p.radius))
+    for k in ("hash", "key", "sorted_ids", "start"):
+        assert np.array_equal(L[k], fx[k]), k

@@ -1,31 +1,32 @@
 """The snapshot file format (csrc/sph_snapshot.cu) as the host-side reader
 fluidsim.snapshot parses it: a file laid out by hand here -- magic, version,
-n, the 13 settings fields, dt, FNV-1a 64 of the payload, then positions,
-velocities and densities -- reads back field for field, and damaged files
-are refused."""
+n, the 13 settings fields, dt, FNV-1a 64 of the header's first 72 bytes and
+the payload (version 2; version 1 covered the payload alone), then
+positions, velocities and densities -- reads back field for field, and
+damaged files, a flipped setting included, are refused."""
 import struct
 
 import numpy as np
 import pytest
 
 
-def make_file(path, n=5, seed=1, bad_digest=False):
+def make_file(path, n=5, seed=1, bad_digest=False, version=2):
     rng = np.random.default_rng(seed)
     pos = rng.normal(size=(n, 3)).astype(np.float32)
     vel = rng.normal(size=(n, 3)).astype(np.float32)
     dens = rng.uniform(1, 50, size=(n, 2)).astype(np.float32)
     payload = pos.tobytes() + vel.tobytes() + dens.tobytes()
+    head72 = (b"SPHSNAP1" + struct.pack("<II", version, n) +
+              struct.pack("<7f", 0.35, 0.1225, 55.0, 500.0, 18.0, 0.06, 9.81) +
+              struct.pack("<i", 1) + struct.pack("<5f", 12.0, 8.0, 6.0, 0.95, 1 / 120) +
+              struct.pack("<f", 1 / 60))
+    assert len(head72) == 72
     h = 14695981039346656037
-    for b in payload:
+    for b in (payload if version == 1 else head72 + payload):
         h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
     if bad_digest:
         h ^= 1
-    head = (b"SPHSNAP1" + struct.pack("<II", 1, n) +
-            struct.pack("<7f", 0.35, 0.1225, 55.0, 500.0, 18.0, 0.06, 9.81) +
-            struct.pack("<i", 1) + struct.pack("<5f", 12.0, 8.0, 6.0, 0.95, 1 / 120) +
-            struct.pack("<f", 1 / 60) + struct.pack("<Q", h))
-    assert len(head) == 80
-    path.write_bytes(head + payload)
+    path.write_bytes(head72 + struct.pack("<Q", h) + payload)
     return pos, vel, dens
 
 
@@ -44,7 +45,14 @@ def test_reader_parses_every_field(tmp_path):
     assert np.array_equal(s["dens"], dens)
 
 
-@pytest.mark.parametrize("damage", ["digest", "truncated", "magic", "version"])
+def test_version_1_files_still_read(tmp_path):
+    from fluidsim import snapshot
+    f = tmp_path / "v1.sph"
+    pos, _, _ = make_file(f, version=1)
+    assert np.array_equal(snapshot.read(f, verify=True)["pos"], pos)
+
+
+@pytest.mark.parametrize("damage", ["digest", "truncated", "magic", "version", "setting"])
 def test_damaged_files_are_refused(tmp_path, damage):
     from fluidsim import snapshot
     f = tmp_path / "b.sph"
@@ -56,6 +64,8 @@ def test_damaged_files_are_refused(tmp_path, damage):
         blob[0] ^= 0xFF
     elif damage == "version":
         blob[8] = 7
+    elif damage == "setting":
+        blob[16] ^= 0x01  # a bit of the radius
     f.write_bytes(bytes(blob))
     with pytest.raises(ValueError):
         snapshot.read(f, verify=True)
