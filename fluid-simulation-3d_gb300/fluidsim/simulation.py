@@ -97,7 +97,10 @@ def grid_arrangement(n: int, gap: float = 0.215):
     """Default lattice of InitializeData / GridArrangement
     (physicsWorld.cc:139-142, 518-557), in float32 like the reference."""
     f = np.float32
-    row = int(math.ceil(f(np.power(f(n), f(1.0) / f(3.0)))))
+    # RowSize = ceil(powf(n, 1.0f / 3.0f)): powf is correctly rounded, so the
+    # double-precision power rounded to float32 reproduces it (numpy's own
+    # float32 power differs for n = 27 and n = 1000)
+    row = int(math.ceil(f(float(n) ** float(f(1.0) / f(3.0)))))
     g = f(gap)
     tot = f(row) * g
     ox = f(0) - ((tot - g) / f(2.0))
@@ -113,6 +116,20 @@ def grid_arrangement(n: int, gap: float = 0.215):
                 out[i] = (ox + f(lx) * g, oy - f(ly) * g, oz + f(lz) * g)
                 i += 1
     return out
+
+
+def speed_of(vel):
+    """getSpeed (physicsWorld.cc:172-176) of velocities [..., 3] in float32:
+    glm::length, sqrt((x*x + y*y) + z*z), each step rounded."""
+    v = np.asarray(vel, np.float32)
+    return np.sqrt((v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1]) + v[..., 2] * v[..., 2])
+
+
+def speed_normalized(vel):
+    """getSpeedNormalzied (physicsWorld.cc:178-182) in float32:
+    clamp(|v|, 0, 1.5) / 1.5."""
+    f = np.float32
+    return (np.minimum(np.maximum(speed_of(vel), f(0.0)), f(1.5)) / f(1.5)).astype(np.float32)
 
 
 class FluidSimulation:
@@ -300,10 +317,10 @@ class FluidSimulation:
         return float(self._state()[2][i, 1]) if self._in(i) else 0.0
 
     def getSpeed(self, i):
-        return float(np.linalg.norm(self._state()[1][i])) if self._in(i) else 0.0
+        return float(speed_of(self._state()[1][i])) if self._in(i) else 0.0
 
     def getSpeedNormalzied(self, i):
-        return min(max(self.getSpeed(i), 0.0), 1.5) / 1.5 if self._in(i) else 0.0
+        return float(speed_normalized(self._state()[1][i])) if self._in(i) else 0.0
 
     def getElapsedTimeGravity(self): return self._timers["gravity"]
     def getElapsedTimeSpatial(self): return self._timers["spatial"]

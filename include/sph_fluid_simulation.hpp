@@ -36,6 +36,36 @@ struct Vec4 {
   float x = 0, y = 0, z = 0, w = 0;
 };
 
+// The default lattice of InitializeData (physicsWorld.cc:139-142) with
+// GridArrangement (physicsWorld.cc:518-557): ceil(n^(1/3)) particles a side
+// at `gap`, centred on the origin, y layers from the top, then x, then z;
+// the first n points.
+inline std::vector<Vec3> GridArrangement(uint32_t n, float gap = 0.215f) {
+  const int per_axis =
+      static_cast<int>(std::ceil(std::pow(static_cast<float>(n), 1.0f / 3.0f)));
+  std::vector<Vec3> out(n);
+  uint32_t i = 0;
+  const float total = per_axis * gap;
+  const float ox = 0 - ((total - gap) / 2.0f);
+  const float oy = 0 + (total - gap) / 2.0f;
+  const float oz = 0 - (total - gap) / 2.0f;
+  for (int ly = 0; ly < per_axis; ++ly)
+    for (int lx = 0; lx < per_axis; ++lx)
+      for (int lz = 0; lz < per_axis; ++lz) {
+        if (i >= n) return out;
+        out[i++] = Vec3{ox + lx * gap, oy - ly * gap, oz + lz * gap};
+      }
+  return out;
+}
+
+// getSpeed / getSpeedNormalzied (physicsWorld.cc:172-182): glm::length, i.e.
+// sqrt((x*x + y*y) + z*z), and clamp(|v|, 0, 1.5) / 1.5.
+inline float SpeedOf(const Vec3& v) { return std::sqrt((v.x * v.x + v.y * v.y) + v.z * v.z); }
+inline float SpeedNormalized(const Vec3& v) {
+  const float s = SpeedOf(v);
+  return (s < 0.0f ? 0.0f : (s > 1.5f ? 1.5f : s)) / 1.5f;
+}
+
 class FluidSimulation {
  public:
   FluidSimulation() { sph_default_params(&prm_); }
@@ -58,8 +88,7 @@ class FluidSimulation {
       if (init->size() != n_) throw std::invalid_argument("position count mismatch");
       positions = *init;
     } else {
-      GridArrangement(static_cast<int>(std::ceil(std::pow(static_cast<float>(n_), 1.0f / 3.0f))),
-                      0.215f);
+      positions = sph::GridArrangement(n_);
     }
     Upload();
   }
@@ -81,15 +110,9 @@ class FluidSimulation {
   Vec3 getVelocity(uint32_t i) const { return i < n_ ? velocity_[i] : Vec3{}; }
   float getDensity(uint32_t i) const { return i < n_ ? densities_[2 * i] : 0.0f; }
   float getNearDensity(uint32_t i) const { return i < n_ ? densities_[2 * i + 1] : 0.0f; }
-  float getSpeed(uint32_t i) const {
-    if (i >= n_) return 0.0f;
-    const Vec3& v = velocity_[i];
-    return std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
-  }
+  float getSpeed(uint32_t i) const { return i < n_ ? SpeedOf(velocity_[i]) : 0.0f; }
   float getSpeedNormalzied(uint32_t i) const {
-    if (i >= n_) return 0.0f;
-    const float s = getSpeed(i);
-    return (s < 0.0f ? 0.0f : (s > 1.5f ? 1.5f : s)) / 1.5f;
+    return i < n_ ? SpeedNormalized(velocity_[i]) : 0.0f;
   }
 
   // Device time per phase of the last Update in ms (CUDA events) when
@@ -190,22 +213,6 @@ class FluidSimulation {
     if (sph_phase_times(h_, ms.data()) != SPH_OK) return 0.0;
     return ms[k];
   }
-  // GridArrangement (physicsWorld.cc:518-557): y layers from the top, then
-  // x, then z, centred on the origin.
-  void GridArrangement(int per_axis, float gap) {
-    uint32_t i = 0;
-    const float total = per_axis * gap;
-    const float ox = 0 - ((total - gap) / 2.0f);
-    const float oy = 0 + (total - gap) / 2.0f;
-    const float oz = 0 - (total - gap) / 2.0f;
-    for (int ly = 0; ly < per_axis; ++ly)
-      for (int lx = 0; lx < per_axis; ++lx)
-        for (int lz = 0; lz < per_axis; ++lz) {
-          if (i >= n_) return;
-          positions[i++] = Vec3{ox + lx * gap, oy - ly * gap, oz + lz * gap};
-        }
-  }
-
   sph_params prm_{};
   sph_sim* h_ = nullptr;
   uint32_t n_ = 0;

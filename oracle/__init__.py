@@ -88,6 +88,7 @@ def lib():
             ctypes.POINTER(OracleParams), ctypes.c_uint32, _P, _P, ctypes.c_uint32, _P,
             ctypes.c_double, ctypes.c_int, _P, _P, _P]
         L.sph_oracle_hw_threads.restype = ctypes.c_int
+        L.sph_oracle_speed_normalized.argtypes = [_P, ctypes.c_uint32, _P]
         L.sph_oracle_render.argtypes = [_P, _P, ctypes.c_uint32, _P, _P, ctypes.c_uint32,
                                         ctypes.c_uint32, ctypes.c_float, _P, _P, _P]
         _lib = L
@@ -203,6 +204,15 @@ def subset_visc_f64(params, pred, velp, subset, dt, nthreads=0):
     return dv, absv, dsens
 
 
+def speed_normalized(vel):
+    """The render restatement's speed normalisation of velocities [n, 3]."""
+    vel = np.ascontiguousarray(vel, dtype=np.float32)
+    out = np.empty(vel.shape[0], np.float32)
+    if lib().sph_oracle_speed_normalized(vel.ctypes.data, vel.shape[0], out.ctypes.data) != 0:
+        raise ValueError("oracle speed normalisation failed")
+    return out
+
+
 def hw_threads() -> int:
     return int(lib().sph_oracle_hw_threads())
 
@@ -275,6 +285,39 @@ def ref_update(params, pos, vel, dt, steps):
     ms = np.frombuffer(raw, np.float64, steps, o).copy(); o += 8 * steps
     phase = np.frombuffer(raw, np.float64, 6, o).copy()
     return posF, velF, dens, ms, phase
+
+
+def _ref_run(mode, params, pos, vel, dt=0.0, steps=1):
+    n = pos.shape[0]
+    with tempfile.TemporaryDirectory() as td:
+        fi, fo = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        _write_input(fi, params, pos, vel, dt, steps, 0)
+        subprocess.run([str(REF_DRIVER), mode, fi, fo], check=True)
+        return open(fo, "rb").read()
+
+
+def ref_init(params, n):
+    """The reference's own InitializeData(n) lattice: (positions [n, 3],
+    OutPositions.w [n])."""
+    if not ref_available():
+        raise RuntimeError("reference driver not built (make -C oracle ref)")
+    z = np.zeros((n, 3), np.float32)
+    raw = _ref_run("init", params, z, z)
+    pos = np.frombuffer(raw, np.float32, 3 * n, 0).reshape(n, 3).copy()
+    w = np.frombuffer(raw, np.float32, n, 12 * n).copy()
+    return pos, w
+
+
+def ref_speed(params, vel):
+    """The reference's getSpeed / getSpeedNormalzied for velocities `vel`
+    [n, 3] at indices 0..n (index n is out of range): two float32 [n + 1]."""
+    if not ref_available():
+        raise RuntimeError("reference driver not built (make -C oracle ref)")
+    n = vel.shape[0]
+    raw = _ref_run("speed", params, np.zeros((n, 3), np.float32), vel)
+    sp = np.frombuffer(raw, np.float32, n + 1, 0).copy()
+    nrm = np.frombuffer(raw, np.float32, n + 1, 4 * (n + 1)).copy()
+    return sp, nrm
 
 
 def render(pos, vel, view):

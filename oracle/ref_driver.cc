@@ -19,6 +19,10 @@
 //       before the density pass, giving the canonical bucket order.
 //   mode "update": `steps` calls of the reference's Update(dt) (Gauss-Seidel
 //       viscosity, the reference's own sort), timing each call.
+//   mode "init": the reference's own InitializeData(n) (physicsWorld.cc:
+//       112-147 with GridArrangement :518-557), nothing loaded over it.
+//   mode "speed": getSpeed(i) and getSpeedNormalzied(i) (physicsWorld.cc:
+//       172-182) of the loaded velocities for i = 0..n (i = n is out of range).
 //
 // in.bin : u32 magic 'SPHI', u32 n, u32 steps, u32 flags,
 //          f32 radius, rho0, k, kn, mu, gscale, gravity_on, bx, by, bz, dt,
@@ -29,6 +33,8 @@
 //          pos[3n], vel[3n]
 // out.bin (update):  f32 pos[3n], vel[3n], dens[2n], f64 ms[steps],
 //          f64 phase_ms[6] (last step's reference timers)
+// out.bin (init):    f32 pos[3n], f32 out_w[n] (OutPositions.w)
+// out.bin (speed):   f32 speed[n+1], f32 speed_normalized[n+1]
 #include <algorithm>
 #include <chrono>
 #include <climits>
@@ -200,11 +206,33 @@ int Update(FluidSimulation& S, const Header& h, FILE* out) {
   return 0;
 }
 
+int Init(FluidSimulation& S, const Header& h, FILE* out) {
+  const uint32_t n = h.n;
+  S.InitializeData(static_cast<int>(n));
+  std::vector<float> pos(3 * n), w(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    for (int c = 0; c < 3; ++c) pos[3 * i + c] = S.positions[i][c];
+    w[i] = S.OutPositions[i].w;
+  }
+  Put(out, pos); Put(out, w);
+  return 0;
+}
+
+int Speed(FluidSimulation& S, const Header& h, FILE* out) {
+  std::vector<float> sp(h.n + 1), nrm(h.n + 1);
+  for (uint32_t i = 0; i <= h.n; ++i) {
+    sp[i] = S.getSpeed(i);
+    nrm[i] = S.getSpeedNormalzied(i);
+  }
+  Put(out, sp); Put(out, nrm);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
   if (argc != 4) {
-    fprintf(stderr, "usage: %s substep|update in.bin out.bin\n", argv[0]);
+    fprintf(stderr, "usage: %s substep|update|init|speed in.bin out.bin\n", argv[0]);
     return 2;
   }
   const std::string mode = argv[1];
@@ -224,12 +252,14 @@ int main(int argc, char** argv) {
   fclose(in);
   FluidSimulation& S = FluidSimulation::getInstance();
   Configure(S, h);
-  Load(S, h, pos, vel);
+  if (mode != "init") Load(S, h, pos, vel);
   FILE* out = fopen(argv[3], "wb");
   if (!out) { perror("out"); return 2; }
   int rc = 2;
   if (mode == "substep") rc = Substep(S, h, out);
   else if (mode == "update") rc = Update(S, h, out);
+  else if (mode == "init") rc = Init(S, h, out);
+  else if (mode == "speed") rc = Speed(S, h, out);
   else fprintf(stderr, "unknown mode %s\n", mode.c_str());
   fclose(out);
   return rc;

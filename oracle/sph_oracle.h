@@ -124,6 +124,10 @@ int sph_oracle_render(const float *pos3, const float *vel3, uint32_t n,
                       uint32_t height, float scale, const float *clear,
                       uint8_t *rgba, float *depth);
 
+/* The speed normalisation the render's colours use (getSpeedNormalzied,
+ * physicsWorld.cc:178-182) of velocities vel3 [3n]: out [n]. */
+int sph_oracle_speed_normalized(const float *vel3, uint32_t n, float *out);
+
 /* Number of hardware threads the oracle would use for nthreads <= 0. */
 int sph_oracle_hw_threads(void);
 

@@ -21,9 +21,15 @@
 
 namespace {
 
-uint32_t SpeedColour(float vx, float vy, float vz) {
+// getSpeedNormalzied (physicsWorld.cc:178-182): clamp(glm::length(v), 0,
+// 1.5) / 1.5, the length as sqrt((x*x + y*y) + z*z).
+float SpeedNormalized(float vx, float vy, float vz) {
   const float len = std::sqrt((vx * vx + vy * vy) + vz * vz);
-  const float nrm = std::fmin(std::fmax(len, 0.0f), 1.5f) / 1.5f;
+  return std::fmin(std::fmax(len, 0.0f), 1.5f) / 1.5f;
+}
+
+uint32_t SpeedColour(float vx, float vy, float vz) {
+  const float nrm = SpeedNormalized(vx, vy, vz);
   const float b1 = 0.33f, b2 = 0.66f;
   const float c1[4] = {0.0f, 0.75f, 1.0f, 1.0f};
   const float c2[4] = {0.0f, 1.0f, 0.0f, 1.0f};
@@ -140,3 +146,10 @@ int sph_oracle_render(const float* pos3, const float* vel3, uint32_t n, const fl
 }
 
 }  // extern "C"
+
+extern "C" int sph_oracle_speed_normalized(const float* vel3, uint32_t n, float* out) {
+  if (!vel3 || !out) return -1;
+  for (uint32_t i = 0; i < n; ++i)
+    out[i] = SpeedNormalized(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2]);
+  return 0;
+}

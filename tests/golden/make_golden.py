@@ -7,8 +7,8 @@ are mounted (an x86-64 host: the reference's float->uint32 hash cast wraps
 there, see the oracle's header). The committed .npz files are what the tests
 read; nothing at test time touches the reference.
 
-    python tests/golden/make_golden.py            # all fixtures
-    python tests/golden/make_golden.py --only substep
+    REF=<reference checkout> python tests/golden/make_golden.py   # all fixtures
+    REF=<reference checkout> python tests/golden/make_golden.py --only substep
 """
 from __future__ import annotations
 
@@ -182,11 +182,58 @@ def rollout_fixture(path, checkpoints=(1, 5, 10, 30, 60, 120)):
                        restatement_jacobi=jac), f, indent=1)
 
 
+LATTICE_SIZES = (1, 2, 27, 64, 100, 343, 1000, 16384, 50000)
+
+
+def lattice_fixture(path):
+    """The reference's own InitializeData(n) lattice (RowSize = ceil(n^(1/3)),
+    GridArrangement, gap 0.215) for several n: full positions up to 1000
+    particles, digests and a 512-point sample beyond; OutPositions.w."""
+    out = {}
+    rng = np.random.default_rng(17)
+    for n in LATTICE_SIZES:
+        pos, w = oracle.ref_init(scenes.SimParams(), n)
+        if n <= 1000:
+            out[f"pos_{n}"] = pos
+        else:
+            idx = np.sort(rng.choice(n, 512, replace=False)).astype(np.uint32)
+            out[f"idx_{n}"] = idx
+            out[f"sample_{n}"] = pos[idx]
+            out[f"digest_{n}"] = sha(pos)
+        out[f"w_{n}"] = np.unique(w)
+    np.savez_compressed(path, sizes=np.array(LATTICE_SIZES), **out)
+
+
+def speed_fixture(path):
+    """getSpeed / getSpeedNormalzied of the reference for the velocities of
+    a stepped scene (the first 4096 particles of the 16k dam break after 30
+    of the reference's own Updates, i.e. 10 steps of dt = 1/60 in 3
+    substeps) and of hand-picked edge cases (rest, exactly 1.5, just above,
+    large, negative components); index n is out of range (0)."""
+    sc = scenes.dam_break_16k()
+    dt = sub_dt(sc)
+    _, vel, _, _, _ = oracle.ref_update(sc["params"], sc["pos"], sc["vel"], dt, 30)
+    edge = np.array([[0, 0, 0], [1.5, 0, 0], [0, -1.5, 0], [0, 0, 1.5000001],
+                     [1e-20, 0, 0], [3, -4, 0], [1e6, 1e6, 1e6], [-0.3, 0.4, -1.2],
+                     [0.86602540, 0.86602540, 0.86602540]], np.float32)
+    v = np.concatenate([vel[:4096], edge]).astype(np.float32)
+    sp, nrm = oracle.ref_speed(sc["params"], v)
+    np.savez_compressed(path, vel=v, speed=sp, speed_normalized=nrm)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["substep", "large", "rollout"], default=None)
+    ap.add_argument("--only", choices=["substep", "large", "rollout", "lattice", "speed"],
+                    default=None)
     a = ap.parse_args()
+    # REF (the reference checkout) comes from the environment
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "oracle", "ref"], check=True)
+    if a.only in (None, "lattice"):
+        lattice_fixture(HERE / "lattice_init.npz")
+        print("lattice_init: reference InitializeData lattices", LATTICE_SIZES)
+    if a.only in (None, "speed"):
+        speed_fixture(HERE / "speed_normalized.npz")
+        print("speed_normalized: reference getSpeed / getSpeedNormalzied")
     if a.only in (None, "substep"):
         for sc in [scenes.dam_break_16k()] + edge_scenes():
             ok = substep_fixture(sc, HERE / f"substep_{sc['name']}.npz")

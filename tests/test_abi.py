@@ -67,14 +67,16 @@ def test_invalid_sizes_rejected(built_lib):
 
 
 def test_grid_arrangement_matches_reference_layout():
-    """GridArrangement (physicsWorld.cc:518-557): rows of ceil(N^(1/3)),
-    gap 0.215, y descending from the top, x then z ascending."""
+    """GridArrangement (physicsWorld.cc:518-557): rows of ceil(powf(N, 1/3)),
+    gap 0.215, y descending from the top, x then z ascending. powf(1000,
+    1/3) rounds to 10.000001, so 1000 particles take rows of 11 (the
+    reference's own output, tests/test_reference_pins.py)."""
     from fluidsim import grid_arrangement
     g = grid_arrangement(1000)
     assert g.shape == (1000, 3)
     f = np.float32
-    off = (f(10) * f(0.215) - f(0.215)) / f(2.0)
+    off = (f(11) * f(0.215) - f(0.215)) / f(2.0)
     assert np.array_equal(g[0], np.array([-off, off, -off], np.float32))
     assert g[1, 2] == g[0, 2] + f(0.215)
-    assert g[10, 0] == g[0, 0] + f(0.215)
-    assert g[100, 1] == g[0, 1] - f(0.215)
+    assert g[11, 0] == g[0, 0] + f(0.215)
+    assert g[121, 1] == g[0, 1] - f(0.215)
