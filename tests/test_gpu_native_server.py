@@ -98,3 +98,18 @@ def test_destroy_with_pending_jobs(gpu_lib):
     for r in reqs:
         srv.submit(r.params, r.pos, r.vel, r.dt, r.steps)
     srv.close()                             # returns while jobs are pending
+
+
+def test_dispatcher_over_the_native_server(gpu_lib):
+    """fluidsim.dispatch with the library's serving loop as the backend of
+    each device (one GPU here): every result equals the request run alone."""
+    from fluidsim import dispatch, server
+    reqs = requests(95, 5)
+    disp = dispatch.Dispatcher.native([0], 4 * 3000 * server.bytes_per_particle(),
+                                      max_scenes=16, substeps=3)
+    done, placed = disp.run(reqs)
+    disp.close()
+    assert set(placed.values()) == {0}
+    for r in reqs:
+        for g, w in zip(done[r.rid], server.run_alone(r)):
+            assert np.array_equal(g, w)
