@@ -617,8 +617,15 @@ __global__ void __maxnreg__(32) k_density_walk(const uint2* __restrict__ tiles,
     // square of a rounding error.
     const float cut = S.cut_le, r = S.r;
     const uint32_t cf = kTables == kTablesDirect ? 0u : cell_first[i];
+    const float2 npxy = make_float2(-p.x, -p.y);
     walk_runs<kTables>(S, start, cell_tab, cf, __float_as_uint(me.w), pred, [&](uint32_t j, float4 q) {
-      const float d2 = dist2(q.x - p.x, q.y - p.y, q.z - p.z);
+      // dist2 with (dx, dy) as one packed FP32x2 pair (x and y are adjacent
+      // in the record): every component rounded as the scalar code rounds
+      // it, two instructions fewer per candidate
+      const float2 dxy = __fadd2_rn(make_float2(q.x, q.y), npxy);
+      const float2 sxy = __fmul2_rn(dxy, dxy);
+      const float dz = q.z - p.z;
+      const float d2 = __fadd_rn(__fadd_rn(sxy.x, sxy.y), __fmul_rn(dz, dz));
       if (d2 <= cut && j != i) {
         if (cnt < nbr_cap) {
           *wp = j;
