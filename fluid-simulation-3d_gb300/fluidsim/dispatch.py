@@ -100,11 +100,19 @@ class Dispatcher:
         return pl
 
     def wait(self, rid, timeout=600.0):
+        """The result of request `rid`; its budget is released once collected.
+        A wait that raises (still running after `timeout`, cancelled, failed)
+        keeps it placed: wait again, or forget() it."""
+        pl, n = self._live[rid]
+        res = self.backends[pl.device].wait(pl.job, timeout)
+        self.forget(rid)
+        return res
+
+    def forget(self, rid):
+        """Drop request `rid` from the placement accounting (its budget is
+        free again), e.g. after it was cancelled or failed."""
         pl, n = self._live.pop(rid)
-        try:
-            return self.backends[pl.device].wait(pl.job, timeout)
-        finally:
-            self.used[pl.device] -= n * self.bpp
+        self.used[pl.device] -= n * self.bpp
 
     def run(self, requests):
         """Submit every request (arrival order), then collect: results by

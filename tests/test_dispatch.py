@@ -138,3 +138,20 @@ def test_two_ranks_serve_disjoint_shares(oracle_mod):
     merged = {rid: h for s in shares for rid, h in s.items()}
     for r in reqs:
         assert merged[r.rid] == digest(run_alone(r))
+
+
+def test_failed_wait_keeps_the_budget_until_forgotten():
+    from fluidsim.dispatch import Dispatcher
+
+    class Slow(OracleBackend):
+        def wait(self, job, timeout=600.0):
+            raise TimeoutError("still running")
+
+    reqs = small_requests(2)
+    disp = Dispatcher([Slow(0)], [10_000 * BPP], BPP)
+    pl = disp.submit(reqs[0])
+    with pytest.raises(TimeoutError):
+        disp.wait(pl.rid)
+    assert disp.used == [reqs[0].n * BPP]  # still running: still placed
+    disp.forget(pl.rid)
+    assert disp.used == [0]
