@@ -198,9 +198,14 @@ struct sph_server {
       }
     }
     const Clock::time_point tb = Clock::now();
-    if (rc == SPH_OK && cudaStreamSynchronize(stream) != cudaSuccess) rc = SPH_ERR_CUDA;
+    std::string eerr;
+    if (rc != SPH_OK) {
+      eerr = eng.LastError();
+    } else if (const cudaError_t e = cudaStreamSynchronize(stream); e != cudaSuccess) {
+      rc = SPH_ERR_CUDA;
+      eerr = std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e);
+    }
     const Clock::time_point t1 = Clock::now();
-    const std::string eerr = rc == SPH_OK ? std::string() : std::string(eng.LastError());
 
     lk.lock();
     admit_s += Seconds(ta, tb);
@@ -232,6 +237,17 @@ struct sph_server {
         t_first = t0;
       }
     }
+    if (rc != SPH_OK) {
+      // the step or the round's synchronisation failed: every resident job,
+      // the ones admitted behind it included, ends with the error
+      err = eerr;
+      for (auto& kv : resident) {
+        eng.RemoveScene(kv.first);
+        Finish(kv.second, rc, err);
+      }
+      resident.clear();
+      return;
+    }
     if (stepped.empty()) {
       if (!admitted_any && resident.empty() && !waiting.empty()) {
         // Nothing runs: a waiting job that did not fit an empty engine never
@@ -247,15 +263,6 @@ struct sph_server {
           waiting.clear();
         }
       }
-      return;
-    }
-    if (rc != SPH_OK) {
-      err = eerr;
-      for (auto& kv : resident) {
-        eng.RemoveScene(kv.first);
-        Finish(kv.second, rc, err);
-      }
-      resident.clear();
       return;
     }
     ++steps;
