@@ -5,9 +5,9 @@
 // because they synchronise the whole device and stall the frame; engines that
 // own a fixed memory budget or a pool forbid allocations from plug-ins.
 // sph_spatial_lookup_static serves them: the caller passes its own device
-// buffers for inputs and outputs, and the working memory (histogram, offsets,
-// cursors) is the file-scope array below, 12 B per particle for up to
-// SPH_STATIC_LOOKUP_MAX particles -- 768 KiB that every GPU loading this
+// buffers for inputs and outputs, and the working memory (histogram and
+// bucket cursors) is the file-scope array below, 8 B per particle for up to
+// SPH_STATIC_LOOKUP_MAX particles -- 512 KiB that every GPU loading this
 // library keeps until the process exits.
 //
 // The entry point has no counterpart in the reference; it builds the same
@@ -33,8 +33,8 @@ constexpr uint32_t kMax = SPH_STATIC_LOOKUP_MAX;
 constexpr int kThreads = 1024;
 constexpr int kMaxDevices = 64;
 
-// count | offset | cursor, kMax entries each.
-__device__ __align__(256) uint32_t g_lookup_scratch[3 * kMax];
+// count | cursor, kMax entries each.
+__device__ __align__(256) uint32_t g_lookup_scratch[2 * kMax];
 
 std::mutex g_mu;
 uint32_t* g_scratch_addr[kMaxDevices] = {};
@@ -75,8 +75,7 @@ k_lookup_static(const float* __restrict__ pred3, uint32_t n, float r,
                 uint32_t* __restrict__ ohash, uint32_t* __restrict__ okey,
                 uint32_t* __restrict__ osorted, uint32_t* __restrict__ ostart) {
   uint32_t* cnt = scratch;
-  uint32_t* off = scratch + kMax;
-  uint32_t* cur = scratch + 2 * kMax;
+  uint32_t* cur = scratch + kMax;
   // The array keeps the previous call's contents: clear the histogram.
   for (uint32_t k = threadIdx.x; k < n; k += kThreads) cnt[k] = 0u;
   __syncthreads();
@@ -99,7 +98,6 @@ k_lookup_static(const float* __restrict__ pred3, uint32_t n, float r,
     uint32_t total;
     const uint32_t ex = block_excl_scan_static(c, &total);
     if (k < n) {
-      off[k] = carry + ex;
       cur[k] = carry + ex;
       ostart[k] = c ? carry + ex : 0x7fffffffu;
     }

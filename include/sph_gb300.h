@@ -261,8 +261,8 @@ const char *sph_global_error(void);
  * buffers), the same lookup as the main path: hash[n] and key[n] = hash % n
  * per particle, sorted_ids[n] in (key, index) order and start[n]
  * (0x7fffffff for an empty key) -- all device buffers of the caller. The
- * working memory is one array inside the library of 12 B per particle for
- * at most SPH_STATIC_LOOKUP_MAX particles (768 KiB, held on every GPU that
+ * working memory is one array inside the library of 8 B per particle for
+ * at most SPH_STATIC_LOOKUP_MAX particles (512 KiB, held on every GPU that
  * loads the library until the process exits); larger n is rejected with
  * SPH_ERR_INVALID. The work is linear in n whatever the keys (particles
  * that all share one key included). Nothing is allocated: no cudaMalloc/cudaFree or
