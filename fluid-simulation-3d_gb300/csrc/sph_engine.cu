@@ -14,8 +14,7 @@ namespace {
 
 // The device address of a host array the device can reach directly (pinned
 // memory mapped into its address space) when 16-byte aligned; nullptr for
-// pageable memory, other alignments and nullptr. (Downloads keep the copy
-// engine: SM stores over the host link measured slower than its copies.)
+// pageable memory, other alignments and nullptr.
 template <class T> T* DeviceAlias(T* p) {
   if (!p) return nullptr;
   cudaPointerAttributes a{};
@@ -680,9 +679,26 @@ int Engine::Download(uint32_t id, float* pos3, float* vel3, float* dens2,
     return Fail(SPH_ERR_INVALID, "no such scene");
   const uint32_t n = scenes_[id].n;
   const uint32_t b = old_base_[id];
+  if (!device_ptrs && (pos3 || vel3 || dens2)) {
+    // Pinned, 16-byte aligned outputs: one kernel gathers the rows in caller
+    // order and stores them over the host link itself, 16-byte words per
+    // 32 rows (the slot map goes to the sort's source-slot scratch, which
+    // every substep rewrites before use).
+    float* hp = DeviceAlias(pos3);
+    float* hv = DeviceAlias(vel3);
+    float* hd = DeviceAlias(dens2);
+    if ((!pos3 || hp) && (!vel3 || hv) && (!dens2 || hd)) {
+      SPH_CUDA(launch_export_rows(b, n, d_pos_[cur_], d_vel_[cur_], ctx_.dens_a,
+                                  ctx_.tmp_src + b, hp, hv, hd, st),
+               "export kernel");
+      SPH_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+      return SPH_OK;
+    }
+  }
   float *op = pos3, *ov = vel3, *od = dens2;
-  // Host copies stage through the prediction / post-pressure / density
-  // buffers (16-32 B per slot, rewritten by every substep before use).
+  // Other host memory stages through the prediction / post-pressure /
+  // density buffers (16-32 B per slot, rewritten by every substep before
+  // use) and the copy engine.
   float* scratch = reinterpret_cast<float*>(ctx_.pred);
   float* scratch_v = reinterpret_cast<float*>(ctx_.rec_v);
   float* scratch_d = reinterpret_cast<float*>(ctx_.dens_b);

@@ -1030,6 +1030,77 @@ __global__ void k_export(uint32_t first, uint32_t n,
   }
 }
 
+// Caller index -> slot for scene slots [first, first + n): the inverse of
+// the ids the slots carry.
+__global__ void k_slot_map(uint32_t first, uint32_t n, const float4* __restrict__ pos,
+                           uint32_t* __restrict__ slot_of) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t id = __float_as_uint(pos[first + k].w);
+  if (id < n) slot_of[id] = first + k;
+}
+
+// This lane's W floats of row i0 + lane (lane < rows) into the warp's staging
+// row buffer, then the warp's rows out as 16-byte words: 32 full rows are
+// 8W aligned words (out is 16-byte aligned and i0 a multiple of 32); a
+// partial last group goes out word by word.
+template <int W>
+__device__ __forceinline__ void store_rows(float* buf, float* __restrict__ out, uint32_t i0,
+                                           uint32_t rows, uint32_t lane, const float* v) {
+  if (lane < rows) {
+#pragma unroll
+    for (int c = 0; c < W; ++c) buf[W * lane + c] = v[c];
+  }
+  __syncwarp();
+  float* dst = out + static_cast<uint64_t>(W) * i0;
+  if (rows == 32u) {
+    if (lane < 8u * W)
+      reinterpret_cast<float4*>(dst)[lane] = reinterpret_cast<const float4*>(buf)[lane];
+  } else {
+    for (uint32_t f = lane; f < W * rows; f += 32u) dst[f] = buf[f];
+  }
+  __syncwarp();
+}
+
+// Caller-order rows written straight into host memory the device maps
+// (pinned, 16-byte aligned), a warp per 32 consecutive caller indices: the
+// warp gathers its rows' slots through slot_of and stores whole aligned
+// 16-byte words, so the host link carries full lines (scattered 12-byte row
+// stores over the link run at a tenth of its rate). A caller index whose
+// slot_of entry is not a slot of the scene (ids that are no permutation: the
+// status flags report the lost slot) gets a zero row.
+__global__ void __launch_bounds__(256) k_export_rows(uint32_t first, uint32_t n,
+                                                     const uint32_t* __restrict__ slot_of,
+                                                     const float4* __restrict__ pos,
+                                                     const float4* __restrict__ vel,
+                                                     const float2* __restrict__ dens,
+                                                     float* __restrict__ opos,
+                                                     float* __restrict__ ovel,
+                                                     float* __restrict__ odens) {
+  __shared__ __align__(16) float buf[8][96];
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  const uint32_t i0 = (blockIdx.x * 8u + w) * 32u;
+  if (i0 >= n) return;
+  const uint32_t rows = min(32u, n - i0);
+  const uint32_t s = lane < rows ? slot_of[i0 + lane] : first;
+  const bool ok = lane < rows && s - first < n;
+  if (opos) {
+    const float4 p = ok ? pos[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float v[3] = {p.x, p.y, p.z};
+    store_rows<3>(buf[w], opos, i0, rows, lane, v);
+  }
+  if (ovel) {
+    const float4 q = ok ? vel[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float v[3] = {q.x, q.y, q.z};
+    store_rows<3>(buf[w], ovel, i0, rows, lane, v);
+  }
+  if (odens) {
+    const float2 d = ok ? dens[s] : make_float2(0.f, 0.f);
+    const float v[2] = {d.x, d.y};
+    store_rows<2>(buf[w], odens, i0, rows, lane, v);
+  }
+}
+
 // ------------------------------------------------------ reference lookup
 // The reference's spatial lookup of a captured substep (UpdateSpatialLookup,
 // physicsWorld.cc:466-496) from the predicted positions of the sorted
@@ -1388,6 +1459,16 @@ cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
   if (n == 0) return cudaSuccess;
   k_export<<<(n + 255) / 256, 256, 0, st>>>(first, n, pos, vel, dens, opos,
                                             ovel, odens, oids);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_export_rows(uint32_t first, uint32_t n, const float4* pos,
+                              const float4* vel, const float2* dens, uint32_t* slot_of,
+                              float* opos, float* ovel, float* odens, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_slot_map<<<(n + 255) / 256, 256, 0, st>>>(first, n, pos, slot_of);
+  k_export_rows<<<(n + 255) / 256, 256, 0, st>>>(first, n, slot_of, pos, vel, dens, opos,
+                                                 ovel, odens);
   return cudaGetLastError();
 }
 

@@ -125,6 +125,12 @@ cudaError_t launch_export(uint32_t first, uint32_t n, const float4* pos,
                           const float4* vel, const float2* dens, float* opos,
                           float* ovel, float* odens, uint32_t* oids,
                           cudaStream_t st);
+// The same rows written into host memory the device maps (pinned, every
+// output 16-byte aligned; nullptr outputs are skipped), in caller order,
+// through slot_of[n] (device scratch, overwritten).
+cudaError_t launch_export_rows(uint32_t first, uint32_t n, const float4* pos,
+                              const float4* vel, const float2* dens, uint32_t* slot_of,
+                              float* opos, float* ovel, float* odens, cudaStream_t st);
 cudaError_t launch_export_debug(uint32_t first, uint32_t n, const float4* pos,
                                 const float4* accp, const float4* velp,
                                 const float4* velv, float* oaccp, float* ovelp,

@@ -125,7 +125,9 @@ int sph_step(sph_sim *sim, float dt, int substeps, void *stream);
 /* Read back state in the caller's particle order (host pointers; any may be
  * NULL): pos3/vel3 float[3n], dens2 float[2n] (density, near density of the
  * last substep, getDensity/getNearDensity physicsWorld.cc:161-170).
- * Synchronises `stream`. */
+ * Page-locked outputs that are all 16-byte aligned are written by the device
+ * directly over the host link; other memory goes through device staging and
+ * copies. Synchronises `stream`. */
 int sph_download(sph_sim *sim, float *pos3, float *vel3, float *dens2,
                  void *stream);
 
