@@ -258,6 +258,11 @@ int sph_batch_sync(sph_batch* b, void* stream) {
   return e == cudaSuccess ? SPH_OK : b->eng.CudaFail(e, "cudaStreamSynchronize");
 }
 
+int sph_batch_status(sph_batch* b, uint32_t* flags, void* stream) {
+  if (!b || !flags) return SPH_ERR_INVALID;
+  return b->eng.Status(flags, S(stream));
+}
+
 int sph_batch_step(sph_batch* b, int substeps, void* stream) {
   if (!b) return SPH_ERR_INVALID;
   return b->eng.Step(substeps, S(stream));

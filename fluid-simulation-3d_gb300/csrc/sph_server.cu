@@ -97,6 +97,7 @@ struct sph_server {
   uint64_t submitted = 0, completed = 0, cancelled = 0, failed = 0;
   uint64_t steps = 0, particle_steps = 0;
   double step_s = 0, admit_s = 0, retire_s = 0;  // worker time per activity
+  uint32_t status_flags = 0;  // device status flags of every step so far
   LatencyHistogram step_ms;  // each step weighted by the jobs it advanced
   bool started = false;
   Clock::time_point t_first{}, t_last{};
@@ -205,10 +206,16 @@ struct sph_server {
       rc = SPH_ERR_CUDA;
       eerr = std::string("cudaStreamSynchronize: ") + cudaGetErrorString(e);
     }
+    uint32_t flags = 0;
+    if (rc == SPH_OK && !stepped.empty() && eng.Status(&flags, stream) != SPH_OK) {
+      rc = SPH_ERR_CUDA;
+      eerr = eng.LastError();
+    }
     const Clock::time_point t1 = Clock::now();
 
     lk.lock();
     admit_s += Seconds(ta, tb);
+    status_flags |= flags;
     bool admitted_any = false;
     for (size_t k = 0; k < trying.size(); ++k) {
       const std::shared_ptr<Job>& j = trying[k];
@@ -443,6 +450,7 @@ int sph_server_get_stats(sph_server* s, sph_server_stats* out) {
   out->step_s = s->step_s;
   out->admit_s = s->admit_s;
   out->retire_s = s->retire_s;
+  out->status_flags = s->status_flags;
   return SPH_OK;
 }
 

@@ -32,7 +32,7 @@ EXPORTS = (
     "sph_kernel_launches", "sph_batch_kernel_launches",
     "sph_batch_profile_enable", "sph_batch_phase_times", "sph_set_tuning",
     "sph_get_tuning", "sph_autotune", "sph_spatial_lookup_static",
-    "sph_static_error", "sph_bytes_per_particle", "sph_batch_sync",
+    "sph_static_error", "sph_bytes_per_particle", "sph_batch_sync", "sph_batch_status",
     "sph_render", "sph_batch_render", "sph_save", "sph_load", "sph_batch_save",
     "sph_batch_add_snapshot", "sph_server_create", "sph_server_destroy",
     "sph_server_submit", "sph_server_cancel", "sph_server_wait", "sph_server_get_stats",
@@ -82,7 +82,7 @@ class ServerStats(ctypes.Structure):
                 ("particle_steps_per_s", ctypes.c_double),
                 ("p50_step_ms", ctypes.c_double), ("p99_step_ms", ctypes.c_double),
                 ("step_s", ctypes.c_double), ("admit_s", ctypes.c_double),
-                ("retire_s", ctypes.c_double)]
+                ("retire_s", ctypes.c_double), ("status_flags", ctypes.c_uint32)]
 
 
 _P = ctypes.c_void_p
@@ -153,6 +153,7 @@ def _sig(L):
         "sph_static_error": (ctypes.c_char_p, []),
         "sph_bytes_per_particle": (u64, []),
         "sph_batch_sync": (i, [_P, _P]),
+        "sph_batch_status": (i, [_P, ctypes.POINTER(u32), _P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

@@ -505,6 +505,13 @@ class Batch:
     def sync(self):
         self._check(self._lib.sph_batch_sync(self._h, self._stream))
 
+    def status(self) -> int:
+        """Device status flags of the batch's kernels since the last read
+        (SPH_STATUS_NONFINITE | SPH_STATUS_RANGE; cleared by the read)."""
+        f = ctypes.c_uint32()
+        self._check(self._lib.sph_batch_status(self._h, ctypes.byref(f), self._stream))
+        return int(f.value)
+
     def download(self, sid: int):
         n = self.sizes[int(sid)]
         pos = np.empty((n, 3), np.float32)

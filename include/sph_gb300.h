@@ -33,7 +33,8 @@ extern "C" {
 #define SPH_ERR_NOMEM -3     /* device allocation or budget exhausted     */
 #define SPH_ERR_STATE -4     /* call not valid in the handle's state      */
 #define SPH_ERR_DEVICE -5    /* reserved: no call returns it; kernel
-                                status flags are read with sph_status     */
+                                status flags are read with sph_status and
+                                sph_batch_status                          */
 
 /* Device status flags (sph_status). */
 #define SPH_STATUS_NONFINITE 0x1u  /* a position/velocity became NaN/inf   */
@@ -314,6 +315,10 @@ int sph_batch_sync(sph_batch *b, void *stream);
  * dt / substeps. */
 int sph_batch_step(sph_batch *b, int substeps, void *stream);
 
+/* Device status flags (SPH_STATUS_*) OR-ed by the batch's kernels since the
+ * last call, over every scene (cleared by the read). Synchronises `stream`. */
+int sph_batch_status(sph_batch *b, uint32_t *flags, void *stream);
+
 /* Read one scene back (host pointers, caller order, any may be NULL).
  * Synchronises `stream`. */
 int sph_batch_download(sph_batch *b, uint32_t scene_id, float *pos3,
@@ -366,6 +371,8 @@ typedef struct sph_server_stats {
                       (the admission uploads of the round overlap it)     */
   double admit_s;  /* of which: staging and queueing admitted jobs' inputs */
   double retire_s; /* worker seconds reading finished jobs back           */
+  uint32_t status_flags; /* device status flags (SPH_STATUS_*) raised by any
+                            step so far, read after every step            */
 } sph_server_stats;
 
 int sph_server_create(uint64_t budget_bytes, uint32_t max_scenes, int substeps,

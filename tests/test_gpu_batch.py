@@ -275,3 +275,37 @@ def test_batch_equals_alone_two_lanes_per_particle(gpu_lib):
         for a, w in zip(g, sim.download()):
             assert np.array_equal(a, w)
         sim.close()
+
+
+def test_many_tiny_scenes_equal_alone(gpu_lib):
+    """8,192 ragged scenes of 1 to 40 particles (every tile partial, many
+    scenes of a single particle, 8,192 key tables of one launch): a sample of
+    48, the smallest and largest among them, equals each scene stepped alone
+    bit for bit, and every scene stays finite."""
+    import fluidsim
+    from fluidsim import scenes
+    rng = np.random.default_rng(8192)
+    scs = []
+    for s in range(8192):
+        n = int(rng.integers(1, 41))
+        pos, vel, bound = scenes.fill_box_scene(rng, n, rng.uniform(0.2, 0.6),
+                                                rng.uniform(0.5, 2.0, size=3))
+        p = scenes.SimParams(radius=0.35, bound=bound, **scenes.DAM_CONSTANTS)
+        scs.append(dict(pos=pos, vel=vel, params=p, dt=1.0 / 60.0))
+    sizes = np.array([s["pos"].shape[0] for s in scs])
+    assert sizes.min() == 1 and sizes.max() == 40
+    b = fluidsim.Batch(int(sizes.sum()), 8192)
+    ids = [b.add(s["params"], s["pos"], s["vel"], s["dt"]) for s in scs]
+    for _ in range(3):
+        b.step(3)
+    sample = set(np.random.default_rng(1).choice(8192, 44, replace=False).tolist())
+    sample |= {int(np.argmin(sizes)), int(np.argmax(sizes)),
+               int(np.flatnonzero(sizes == 1)[-1]), int(np.flatnonzero(sizes == 33)[0])}
+    for k, (sid, sc) in enumerate(zip(ids, scs)):
+        got = b.download(sid)
+        assert all(np.isfinite(g).all() for g in got), k
+        if k in sample:
+            for g, r in zip(got, alone(sc, 3)):
+                assert np.array_equal(g, r), k
+    assert b.status() == 0
+    b.close()

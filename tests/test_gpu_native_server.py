@@ -62,6 +62,7 @@ def test_cancel_refuse_and_timeout(gpu_lib):
     assert e.value.code == -3
     st = srv.stats()
     assert st["cancelled"] == 2 and st["completed"] == 2
+    assert st["status_flags"] == 0
     srv.close()
 
 
