@@ -165,19 +165,29 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, interval_ms=200):
         self.gpu = gpu_index
+        self.interval_ms = int(interval_ms)
         self.proc = None
         self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
 
-    def start(self):
+    def start(self, wait_live=False):
+        """Start sampling; with wait_live, return once the first sample is
+        written (at most 3 s), so a short region that follows is covered."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.interval_ms)],
                 stdout=self.tmp, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        t0 = time.perf_counter()
+        while wait_live and time.perf_counter() - t0 < 3.0:
+            self.tmp.flush()
+            if os.path.getsize(self.tmp.name) > 0:
+                break
+            time.sleep(0.01)
 
     def stop(self):
         if self.proc is None:
@@ -424,10 +434,11 @@ def run_native(args):
         total_ms = float(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)))
         return total_ms, wall, launches, phase
 
-    clocks = ClockSampler(local)
-    clocks.start()
+    # clocks over the GPU work of the timed, profiled and end-to-end passes
+    # (the timed pass alone is shorter than one sampling interval)
+    clocks = ClockSampler(local, interval_ms=20)
+    clocks.start(wait_live=True)
     rank_ms, wall, launches, _ = timed_pass(False)
-    clk = clocks.stop()
     value, total_ms = replica_throughput(n, args.steps, rank_ms, world, "cuda")
     prof_ms, _, _, phase = timed_pass(True)
     prof_ms = max_over_ranks(prof_ms, world, "cuda")
@@ -470,6 +481,10 @@ def run_native(args):
         e2e_local += time.perf_counter() - t0
     e2e_s = max_over_ranks(e2e_local, world, "cuda")
     e2e_value = world * n * e2e_steps / e2e_s
+    clk = clocks.stop()
+    if clk:
+        clk["window"] = ("20 ms samples over the timed, profiled and end-to-end "
+                         "passes (warm-up steps included)")
     render_block = time_render(sim, sc, stream, args.warmup)
     sim_tuning = sim.tuning()
     sim.close()
