@@ -591,15 +591,22 @@ def run_native(args):
                       f"{args.warmup} untimed ones ({steps * S} substeps), "
                       f"{el:.1f} s on {th} threads"}
     if world == 1 and not args.no_batched:
-        # config 2, one GPU's form (each block samples its own clocks)
+        # config 2, one GPU's form (each block samples its own clocks); a
+        # block that fails is reported in the line, which is still printed
         ck = ClockSampler(local)
         ck.start()
-        line["batched"] = batched_block(args, stream)
+        try:
+            line["batched"] = batched_block(args, stream)
+        except Exception as e:  # noqa: BLE001 -- reported, not hidden
+            line["batched"] = {"error": f"{type(e).__name__}: {e}"}
         line["batched"]["clocks"] = ck.stop()
     if world == 1 and not args.no_served:
         ck = ClockSampler(local)
         ck.start()
-        line["served"] = served_block(args)
+        try:
+            line["served"] = served_block(args)
+        except Exception as e:  # noqa: BLE001 -- reported, not hidden
+            line["served"] = {"error": f"{type(e).__name__}: {e}"}
         line["served"]["clocks"] = ck.stop()
     print(json.dumps(line), flush=True)
     if world > 1:
